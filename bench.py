@@ -1,0 +1,305 @@
+"""Benchmark: particle-steps/s of the full SPH warm-rain step.
+
+Workload: the 2,097,152-particle moist-bubble configuration (cfg1:
+128^3 jittered lattice in a 20 x 20 x 8 km box, cells 150.4 x 150.4 x 40 m,
+three seeded warm bubbles, warm rain with accretion and evaporation, Morton
+re-sort every step).  Synthetic, seeded initial state; no dataset.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours: K fused steps (sort + gather/kick/drift/flux + density/EOS/micro +
+momentum/integrate/rain/CFL, one CUDA graph per step) timed with CUDA events
+on the simulation stream; one JSON line on rank 0.  --impl reference times
+the CPU restatement of the reference (FP64, all host cores) on a bounded
+sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s (plain step, 2,097,152 particles)"
+UNIT = "particle-steps/s"
+L2_BYTES = 129e6
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(N: int, C: int) -> dict:
+    """Minimum compulsory traffic of the reference dataflow per step with a
+    sort every step (bytes): keygen 16 + sort 16 + gather 108 + table 4 +
+    8 per cell + kick/drift 60 + density/EOS/micro 48 + momentum/integrate
+    72 + rain 12 per cell (per particle unless noted)."""
+    per_particle = 16 + 16 + 108 + 4 + 60 + 48 + 72
+    return {"step": per_particle * N + 20 * C,
+            "momentum_integrate": 72 * N + 12 * C,
+            "density_eos": 48 * N,
+            "gather_kick_drift": (108 + 60 + 16) * N,
+            "sort": 16 * N,
+            "table_clear": 8 * C}
+
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": float(np.median(load)), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_sample_params():
+    """cfg1 physics on a quarter-width box: 32 x 32 x 128 lattice (131,072
+    particles), 33 x 33 x 200 cells of the same 150.4 x 150.4 x 40 m size, so
+    the per-particle neighbour work equals the full workload's."""
+    import sph_cuda_gb300 as sph
+    p = sph.preset("cfg1")
+    p.nx = p.ny = 33
+    p.lat_nx = p.lat_ny = 32
+    p.n_particles = 32 * 32 * 128
+    for b in range(p.n_bubbles):
+        p.bubble_x[b] *= 33 / 133.0
+        p.bubble_y[b] *= 33 / 133.0
+    return p
+
+
+def time_oracle(p, state, nsteps: int):
+    from oracle import oracle
+    t0 = time.perf_counter()
+    _, _, _, ctl, st = oracle.run(p, state, nsteps)
+    dt = time.perf_counter() - t0
+    return dt, oracle.threads(), st
+
+
+def oracle_initial_state(p):
+    """Initial state of the CPU runs from the oracle's own init."""
+    from oracle import oracle
+    return oracle.init_state(p)
+
+
+def run_reference(args):
+    ws, rank, local = dist_setup()
+    if rank != 0:
+        return 0
+    from oracle import oracle
+    p = cpu_sample_params()
+    state = oracle_initial_state(p)
+    # one warm-up step, then K timed steps, each one full FP64 step of the sample
+    oracle.run(p, state, 1)
+    t, cores, _ = time_oracle(p, state, args.steps)
+    value = p.n_particles * args.steps / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": "cfg1 moist bubble (sample: 131,072-particle quarter box)",
+                                       "particles": p.n_particles, "cells": p.nx * p.ny * p.nz},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d full FP64 steps of the 131,072-particle quarter-box cfg1 sample" % args.steps},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import sph_cuda_gb300 as sph
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.Stream()
+    p = sph.preset("cfg1")
+    N, C = p.n_particles, p.nx * p.ny * p.nz
+    sim = sph.Asph(p, stream=stream.cuda_stream)
+    sim.init()
+    bits = 1
+    while (1 << bits) < max(p.nx, p.ny, p.nz):
+        bits += 1
+    npasses = (3 * bits + 7) // 8
+    launches_per_step = 5 + npasses   # table clear, histogram, passes, gather, density, momentum
+    sim.step(max(args.warmup, 1))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.step_async(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    sim.sync()
+    clk = clocks.stop()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    value = ws * N * args.steps / (ms / 1e3)
+
+    # per-kernel device times of the same step (non-graph launches, events
+    # between the kernels on the simulation stream)
+    prof_steps = max(3, min(args.steps, 20))
+    ph = sim.step_profiled(prof_steps)
+    ph_ms = {k: v / prof_steps for k, v in ph.items()}
+    algo = algorithmic_bytes(N, C)
+    kernels = ["table_clear", "sort", "gather_kick_drift", "density_eos", "momentum_integrate"]
+    dom = max(kernels, key=lambda k: ph_ms[k])
+    hbm, src = peaks()
+    achieved = algo[dom] / (ph_ms[dom] / 1e3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic_cfg1.json.txt")
+    if os.path.exists(tfile):
+        try:
+            traffic = json.load(open(tfile)).get(dom)
+        except Exception:
+            traffic = None
+
+    # end to end through the C ABI with pinned host buffers: per step the
+    # persistent state goes host->device, one step runs, the state comes back
+    fields = ("x", "y", "z", "u", "v", "w", "th", "qv", "qc", "rho", "ax", "ay", "az")
+    host = {k: torch.empty(N, dtype=torch.float32, pin_memory=True).numpy() for k in fields}
+    sim.get_state(fields, out=host)
+    e2e_steps = max(3, min(args.steps, 20))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.set_state(host)
+        sim.step(1)
+        sim.get_state(fields, out=host)
+    t_e2e = time.perf_counter() - t0
+    tt = torch.tensor([t_e2e], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    e2e = ws * N * e2e_steps / float(tt.item())
+    nbytes = len(fields) * 4 * N
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        ps = cpu_sample_params()
+        st = oracle_initial_state(ps)
+        tc, cores, _ = time_oracle(ps, st, args.cpu_steps)
+        cpu = {"value": ps.n_particles * args.cpu_steps / tc, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "%d full FP64 steps of the 131,072-particle quarter-box cfg1 sample (%.1f s)"
+                         % (args.cpu_steps, tc)}
+
+    ctl = sim.control()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "cfg1 moist bubble, 2,097,152 particles, 133x133x200 cells, sort every step",
+                       "particles": N, "cells": C, "dt_s": ctl["dt"],
+                       "l2": "working set %.0f MB > 129 MB L2 (no flush needed)" % ((N * 164 + C * 20) / 1e6),
+                       "parallelism": "replicas x%d" % ws},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
+                         "step_achieved": algo["step"] / (ph_ms["step"] / 1e3) / 1e9,
+                         "kernel_ms": ph_ms},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                    "steps": e2e_steps, "api": "asph_set_state + asph_step(1) + asph_get_state, pinned host SoA"},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk,
+            "state": {"simt": ctl["simt"], "steps_done": ctl["step"], "aborted": ctl["aborted"],
+                      "wmax": ctl["wmax"]},
+        }
+        print(json.dumps(line))
+    sim.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,225 @@
+/*
+ * asph.h — C ABI of the GB300 anisotropic-SPH warm-rain step.
+ *
+ * The reference (Forbu/sph_cuda, a single file asph_h100.cu) has no library
+ * interface: its boundaries are (1) the CLI flags and the asph_tXXXXXXs.bin
+ * dump files written by main() (asph_h100.cu:753-1176) and (2) the raw
+ * kernel launches of its host loop (asph_h100.cu:958-1161).  Every entry
+ * point below replaces one block of that host loop; the comment on each
+ * names the reference lines it stands for.
+ *
+ * Conventions
+ *  - Plain C types only: no CUDA or torch types appear in a signature.  A
+ *    stream is passed as `void*` holding a cudaStream_t (NULL = the legacy
+ *    default stream, which is what the reference uses).
+ *  - Every call returns an `int` status (ASPH_OK or an ASPH_ERR_* code) and
+ *    never calls exit(); asph_last_error() gives a one-line reason for the
+ *    last failure on the calling thread.
+ *  - The context owns all device memory.  Host buffers passed to get/set
+ *    calls are caller-owned and are copied; pinned host memory makes the
+ *    copies asynchronous-capable but is not required.
+ *  - One context belongs to one stream and is not thread-safe; distinct
+ *    contexts may be driven from distinct threads.
+ *  - Particle fields are float32, stored on the device as 16-byte field
+ *    groups (pos = x,y,z,rho_old ; vel = u,v,w,- ; thq = theta,qv,qc,-) in
+ *    Morton order, the layout the reference uses (asph_h100.cu:829-838).
+ */
+#ifndef ASPH_H_
+#define ASPH_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ASPH_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define ASPH_OK             0
+#define ASPH_ERR_CUDA       1   /* a CUDA runtime call failed (reference: CK -> exit 1, asph_h100.cu:41-43) */
+#define ASPH_ERR_CONFIG     2   /* invalid parameters (reference: Morton limit -> exit 1, asph_h100.cu:785-788) */
+#define ASPH_ERR_CFL_ABORT  3   /* CFL trip limit exceeded (reference: return 2, asph_h100.cu:1061-1066) */
+#define ASPH_ERR_TIMEOUT    4   /* a bounded device-side wait gave up */
+#define ASPH_ERR_ARG        5   /* NULL pointer / bad argument */
+#define ASPH_ERR_NOMEM      6   /* device or host allocation failed */
+#define ASPH_ERR_IO         7   /* dump file could not be written */
+#define ASPH_ERR_STATE      8   /* call out of order (e.g. step before init) */
+
+/* ---- parameter presets ------------------------------------------------- */
+#define ASPH_PRESET_REFERENCE 0 /* the reference's constexpr physics, 1 particle per cell (asph_h100.cu:48-120) */
+#define ASPH_PRESET_CFG0      1 /* 65,536 particles, 10x10x5 km, h 200/50 m, one bubble */
+#define ASPH_PRESET_CFG1      2 /* 2,097,152 particles, 20x20x8 km, h 150/40 m, three bubbles, sort every step */
+#define ASPH_PRESET_CFG2      3 /* 16,777,216 particles, 40x40x10 km, h 160/20 m, 95% RH below 1 km */
+#define ASPH_PRESET_CFG3      4 /* 262,144 particles in the CFG0 box (adjoint workload) */
+
+#define ASPH_INIT_REFERENCE 0   /* one particle at each cell centre + hash noise (asph_h100.cu:210-227) */
+#define ASPH_INIT_LATTICE   1   /* jittered lattice + Gaussian bubbles + Gaussian noise */
+
+#define ASPH_QV_REFERENCE 0     /* qv_ref = qv0 exp(-z/2500) exp(-max(z-5000,0)/1000) (asph_h100.cu:149-153) */
+#define ASPH_QV_RH        1     /* qv_ref = RH(z) * qsat(T_ref, p_ref) */
+
+#define ASPH_MAX_BUBBLES 8
+
+/* Every constexpr of asph_h100.cu:48-120 becomes a runtime field. */
+typedef struct AsphParams {
+    /* grid (asph_h100.cu:48-57): cells per axis; the cell edge is the kernel
+     * length on that axis, the support is 2 cells (q < 2) */
+    int32_t nx, ny, nz;
+    float   dx, dy, dz;
+    /* particles and initial state */
+    int32_t n_particles;
+    int32_t init_mode;                 /* ASPH_INIT_* */
+    int32_t lat_nx, lat_ny, lat_nz;    /* ASPH_INIT_LATTICE: lattice counts, product = n_particles */
+    float   jitter;                    /* uniform jitter as a fraction of the lattice spacing */
+    uint32_t seed;
+    float   noise;                     /* REFERENCE: hash-noise amplitude [K] (--noise); LATTICE: Gaussian sigma [K] */
+    int32_t n_bubbles;
+    float   bubble_x[ASPH_MAX_BUBBLES], bubble_y[ASPH_MAX_BUBBLES], bubble_z[ASPH_MAX_BUBBLES];
+    float   bubble_r[ASPH_MAX_BUBBLES], bubble_amp[ASPH_MAX_BUBBLES];  /* theta' = amp exp(-(d/r)^2) */
+    /* sounding (asph_h100.cu:66-76, 136-153) */
+    float   th0, n2, cs;
+    int32_t qv_mode;                   /* ASPH_QV_* */
+    float   qv0, rh, rh_bl, z_bl;      /* RH(z) = rh_bl below z_bl, rh above */
+    /* dissipation (asph_h100.cu:84-91) */
+    float   alpha_av, beta_av, h_av;   /* beta_av = 0 reproduces the reference exactly */
+    float   sponge_sigma, sponge_frac, dthdt_cap;
+    /* surface forcing (asph_h100.cu:100-105) */
+    int32_t surface_flux;
+    float   c_h, c_e, beta_moist, v_bg, dts_skin, ramp;
+    /* warm-rain microphysics (asph_h100.cu:111-120) */
+    float   qc_auto, rate_auto, v_rain, theta_cap, qv_cap;
+    int32_t accretion, rain_evap;      /* Kessler accretion / rain evaporation (absent in the reference: 0) */
+    float   k_accr;                    /* accretion rate constant [1/s] */
+    /* time stepping and CFL control (asph_h100.cu:728-742, 794-797, 1040-1078) */
+    float   dt_request;                /* --dt ; <= 0 means the static bound */
+    float   cfl;
+    int32_t max_trip, strict_cfl;
+    int32_t adaptive_dt;               /* 1: adopt the closed-loop dt (reference); 0: keep dt fixed */
+    int32_t sort_every;                /* 0: displacement-gated cadence (reference); k>0: every k steps */
+    int32_t permute_acc;               /* 0: reference (acc keeps its pre-sort order); 1: acc follows its particle */
+    float   pmass;                     /* particle mass [kg]; 0: rho0 * Lx*Ly*Lz / n_particles */
+    /* coarse dump strides (asph_h100.cu:737) */
+    int32_t dump_sx, dump_sy, dump_sz;
+    int32_t reserved[16];
+} AsphParams;
+
+/* Host-side SoA view of the particle state, in the context's current
+ * (Morton-sorted) order.  Any pointer may be NULL to skip that field. */
+typedef struct AsphHostState {
+    float *x, *y, *z;       /* position [m] */
+    float *u, *v, *w;       /* velocity [m/s] */
+    float *th, *qv, *qc;    /* potential temperature [K], vapour and cloud water [kg/kg] */
+    float *rho;             /* current density [kg/m^3] */
+    float *ax, *ay, *az;    /* last acceleration [m/s^2] (needed by the first half kick) */
+    float *prs;             /* perturbation pressure p' [Pa] */
+    float *dthdt;           /* viscous-heating tendency [K/s] */
+} AsphHostState;
+
+/* Device control block: the values the reference keeps in host variables
+ * of its step loop (asph_h100.cu:931-942, 1040-1078). */
+typedef struct AsphControl {
+    double  simt;           /* simulated time [s] */
+    double  since_sort;     /* time since the last sort [s] */
+    float   dt;             /* dt of the next step [s] */
+    float   dt_cap, dt_floor, dt_static;
+    float   dt_required;    /* last closed-loop CFL bound */
+    float   sort_dt;        /* displacement-gated sort interval [s] */
+    float   umax, vmax, wmax;  /* last |u|,|v|,|w| maxima */
+    int32_t step;           /* completed steps */
+    int32_t trips;          /* consecutive CFL violations */
+    int32_t sort_count;
+    int32_t aborted;        /* 1 after a CFL abort: later steps do nothing */
+    int32_t clamp_pending;  /* a CFL trip asked for the velocity clamp */
+    int32_t do_sort;        /* the next step starts with a sort */
+    int32_t error;          /* device error word (ASPH_ERR_TIMEOUT ...) */
+    int32_t surf_count;     /* particles in the lowest layer at the last sort */
+} AsphControl;
+
+/* ---- library / parameters ---------------------------------------------- */
+int         asph_abi_version(void);
+/* sizeof(AsphParams) as compiled into the library (FFI layout check). */
+int         asph_params_size(void);
+const char* asph_last_error(void);
+const char* asph_status_string(int status);
+/* Fill `p` with a preset.  nx,ny,nz > 0 override the preset grid (used by
+ * ASPH_PRESET_REFERENCE, which mirrors --nx/--ny/--nz, asph_h100.cu:760-762). */
+int asph_params_preset(AsphParams* p, int preset, int nx, int ny, int nz);
+/* Validate parameters (Morton limit 1024 cells/axis, asph_h100.cu:785-788). */
+int asph_params_check(const AsphParams* p);
+
+/* ---- context ------------------------------------------------------------ */
+typedef struct asph_ctx asph_ctx;
+/* Allocate every device buffer the reference allocates (asph_h100.cu:827-872). */
+int asph_create(const AsphParams* p, void* stream, asph_ctx** out);
+int asph_destroy(asph_ctx* ctx);
+/* Initial state, initial sort, initial force evaluation
+ * (asph_h100.cu:885-921): kernel_init, kernel_iota, sort, density,
+ * kernel_eos_micro, kernel_momentum. */
+int asph_init(asph_ctx* ctx);
+/* Replace the particle state with host arrays (x..qc and rho required, the
+ * rest optional) and reset the cell table; the next sort rebuilds it. */
+int asph_set_state(asph_ctx* ctx, const AsphHostState* st);
+int asph_get_state(asph_ctx* ctx, AsphHostState* st);
+/* Rain grid (nx*ny*nz cells) and surface precipitation (nx*ny). */
+int asph_get_rain(asph_ctx* ctx, float* rain, float* precip2d);
+int asph_set_rain(asph_ctx* ctx, const float* rain, const float* precip2d);
+int asph_get_control(asph_ctx* ctx, AsphControl* c);
+/* Set simt, dt and the sort flag (tests and restarts). */
+int asph_set_time(asph_ctx* ctx, double simt, float dt, int do_sort);
+
+/* ---- granular steps (one block of the reference step each) -------------- */
+/* keys -> stable radix sort -> gather -> cell table + surface list
+ * (asph_h100.cu:963-977: kernel_morton_keys, SortPairs, kernel_gather,
+ * memset, kernel_build_pairs). */
+int asph_sort_build(asph_ctx* ctx);
+/* Sort outputs: unsorted keys of the pre-sort order, sorted keys, the
+ * permutation, cellRange (2*nx*ny*nz ints: start,end per cell, {0,0} for an
+ * empty cell) and the surface list in ascending order. */
+int asph_get_sort(asph_ctx* ctx, uint32_t* keys_in, uint32_t* keys_sorted,
+                  uint32_t* perm, int32_t* cell_range, int32_t* surf_list,
+                  int32_t* surf_count);
+/* half kick + drift + surface flux (asph_h100.cu:981-998). */
+int asph_kick_drift_flux(asph_ctx* ctx);
+/* summation density + EOS + saturation adjustment + autoconversion
+ * (+ accretion/evaporation when enabled) (asph_h100.cu:1002-1008). */
+int asph_density_eos(asph_ctx* ctx);
+/* momentum (asph_h100.cu:1013); with integrate != 0 also theta update,
+ * second half kick and sponge (asph_h100.cu:1019-1026). */
+int asph_momentum(asph_ctx* ctx, int integrate);
+/* rain sedimentation (asph_h100.cu:1028-1036). */
+int asph_rain(asph_ctx* ctx);
+/* closed-loop CFL control on the device (asph_h100.cu:1040-1078). */
+int asph_cfl(asph_ctx* ctx);
+/* nsteps full steps (asph_h100.cu:958-1078) as one CUDA graph per step
+ * pair, no host synchronisation inside; returns ASPH_ERR_CFL_ABORT if the
+ * trip limit was exceeded during the call. */
+int asph_step(asph_ctx* ctx, int nsteps);
+/* Queue nsteps without waiting; asph_sync() collects the status. */
+int asph_step_async(asph_ctx* ctx, int nsteps);
+int asph_sync(asph_ctx* ctx);
+
+/* nsteps steps launched without a graph, with CUDA events between the
+ * phases (the reference's per-phase timers, asph_h100.cu:931-954, 1149-1157).
+ * phase_ms[ASPH_NPHASES] receives the summed milliseconds of: 0 cell-table
+ * clear + sort reset, 1 digit histogram + radix passes, 2 gather / kick /
+ * drift / flux / keys, 3 density + EOS + microphysics, 4 momentum +
+ * integration + rain + CFL, 5 the whole step. */
+#define ASPH_NPHASES 6
+int asph_step_profiled(asph_ctx* ctx, int nsteps, float* phase_ms);
+
+/* ---- diagnostics and output ----------------------------------------------- */
+/* FP64 totals: KE, PE, IE, water, p_z, mass (asph_h100.cu:650-668). */
+int asph_audit(asph_ctx* ctx, double out[6]);
+/* Coarse dump in the reference format (asph_h100.cu:1080-1120), file name
+ * <outdir>/asph_t%06.0fs.bin; `path` (may be NULL) receives the name. */
+int asph_dump(asph_ctx* ctx, const char* outdir, char* path, int path_len);
+/* Column diagnostics of the dump line (asph_h100.cu:1095-1105): cloud
+ * cover [%], max ql [kg/kg], max |w| [m/s], mean precipitation [mm];
+ * resets the precipitation accumulator like the reference. */
+int asph_column_diag(asph_ctx* ctx, float out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ASPH_H_ */

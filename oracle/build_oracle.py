@@ -1,0 +1,86 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+* liboracle.so  — the FP64 C restatement (asph_oracle.c), gcc + OpenMP.
+* _ref/asph_ref.cubin — the reference's device code compiled UNMODIFIED
+  from the reference checkout with its own documented flags
+  (asph_h100.cu:23-25: -O3 -use_fast_math -std=c++17), retargeted to
+  sm_103a.  Built only where the reference checkout exists; the cubin is
+  architecture-neutral for the host, so it travels to the GPU machine.
+* refgpu — host program that loads that cubin and replays the reference
+  step (refgpu.cu); compiled wherever nvcc and libcuda are available.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_OUT = os.path.join(HERE, "_ref")
+REFERENCE_SRC = os.environ.get("ASPH_REFERENCE_SRC", "/root/reference/asph_h100.cu")
+LIBORACLE = os.path.join(BUILD, "liboracle.so")
+CUBIN = os.path.join(REF_OUT, "asph_ref.cubin")
+REFGPU = os.path.join(BUILD, "refgpu")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+
+
+def _stale(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def build_oracle(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "asph_oracle.c")
+    hdr = os.path.join(os.path.dirname(HERE), "include", "asph.h")
+    if force or _stale(LIBORACLE, [src, hdr]):
+        _run(["gcc", "-O2", "-std=c11", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
+              "-o", LIBORACLE, src, "-lm"])
+    return LIBORACLE
+
+
+def build_ref_cubin(force: bool = False) -> str:
+    """Compile the reference's kernels into a cubin (needs the checkout)."""
+    if not os.path.exists(REFERENCE_SRC):
+        return CUBIN if os.path.exists(CUBIN) else ""
+    os.makedirs(REF_OUT, exist_ok=True)
+    if force or _stale(CUBIN, [REFERENCE_SRC]):
+        _run([_nvcc(), "-cubin", "-O3", "-use_fast_math", "-std=c++17", *ARCH, "-o", CUBIN, REFERENCE_SRC])
+    return CUBIN
+
+
+def build_refgpu(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "refgpu.cu")
+    if force or _stale(REFGPU, [src]):
+        stubs = "/usr/local/cuda/lib64/stubs"
+        _run([_nvcc(), "-O2", "-std=c++17", *ARCH, "-o", REFGPU, src, "-lcuda", "-L", stubs])
+    return REFGPU
+
+
+def build_all(force: bool = False) -> None:
+    build_oracle(force)
+    build_ref_cubin(force)
+    build_refgpu(force)
+
+
+if __name__ == "__main__":
+    build_all(force="--force" in sys.argv)
+    print(LIBORACLE, CUBIN, REFGPU)

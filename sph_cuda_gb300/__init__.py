@@ -1,0 +1,211 @@
+"""GB300 anisotropic-SPH warm-rain step (Forbu/sph_cuda asph_h100.cu hot path).
+
+Python host mirror of the C ABI in include/asph.h.  Every method is one C
+call into libasph.so; there is no Python or CPU implementation of any step,
+so a missing or unloadable library raises immediately.
+
+    p = sph_cuda_gb300.preset("cfg1")
+    sim = sph_cuda_gb300.Asph(p)
+    sim.init()
+    sim.step(500)
+    state = sim.get_state()
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import (AsphControl, AsphHostState, AsphParams, STATE_FIELDS, load_library)
+
+__all__ = ["Asph", "AsphError", "AsphParams", "preset", "library", "STATE_FIELDS"]
+
+PRESETS = {
+    "reference": abi.PRESET_REFERENCE,
+    "cfg0": abi.PRESET_CFG0,
+    "cfg1": abi.PRESET_CFG1,
+    "cfg2": abi.PRESET_CFG2,
+    "cfg3": abi.PRESET_CFG3,
+}
+
+
+class AsphError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("asph status %d: %s" % (status, msg))
+        self.status = status
+
+
+def library() -> C.CDLL:
+    return load_library()
+
+
+def _check(st: int) -> None:
+    if st != abi.ASPH_OK:
+        lib = library()
+        raise AsphError(st, (lib.asph_last_error() or b"").decode(errors="replace")
+                        or lib.asph_status_string(st).decode())
+
+
+def preset(name: str = "cfg1", nx: int = 0, ny: int = 0, nz: int = 0, **overrides) -> AsphParams:
+    """Fill AsphParams from a named preset, then apply field overrides."""
+    p = AsphParams()
+    _check(library().asph_params_preset(C.byref(p), PRESETS[name], nx, ny, nz))
+    for k, v in overrides.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def check_params(p: AsphParams) -> None:
+    _check(library().asph_params_check(C.byref(p)))
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Asph:
+    """One simulation context (device buffers, stream, captured graphs)."""
+
+    def __init__(self, params: AsphParams, stream: int | None = None):
+        self.lib = library()
+        self.params = params.copy()
+        self._ctx = C.c_void_p()
+        _check(self.lib.asph_create(C.byref(self.params), C.c_void_p(stream or 0), C.byref(self._ctx)))
+        self.N = int(self.params.n_particles)
+        self.ncell = int(self.params.nx * self.params.ny * self.params.nz)
+
+    def close(self) -> None:
+        if self._ctx:
+            self.lib.asph_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- state --------------------------------------------------------------
+    def init(self) -> None:
+        _check(self.lib.asph_init(self._ctx))
+
+    def set_state(self, fields: dict) -> None:
+        hs = AsphHostState()
+        keep = []
+        for name in STATE_FIELDS:
+            if name in fields and fields[name] is not None:
+                a = np.ascontiguousarray(fields[name], dtype=np.float32)
+                if a.shape != (self.N,):
+                    raise ValueError("field %s has shape %s, expected (%d,)" % (name, a.shape, self.N))
+                keep.append(a)
+                setattr(hs, name, _fptr(a))
+        _check(self.lib.asph_set_state(self._ctx, C.byref(hs)))
+
+    def get_state(self, fields=STATE_FIELDS, out: dict | None = None) -> dict:
+        hs = AsphHostState()
+        res = {}
+        for name in fields:
+            a = out[name] if out is not None and name in out else np.empty(self.N, np.float32)
+            res[name] = a
+            setattr(hs, name, _fptr(a))
+        _check(self.lib.asph_get_state(self._ctx, C.byref(hs)))
+        return res
+
+    def get_rain(self):
+        rain = np.empty(self.ncell, np.float32)
+        precip = np.empty(self.params.nx * self.params.ny, np.float32)
+        _check(self.lib.asph_get_rain(self._ctx, _fptr(rain), _fptr(precip)))
+        return rain, precip
+
+    def set_rain(self, rain=None, precip=None) -> None:
+        r = None if rain is None else np.ascontiguousarray(rain, np.float32)
+        q = None if precip is None else np.ascontiguousarray(precip, np.float32)
+        _check(self.lib.asph_set_rain(self._ctx, _fptr(r) if r is not None else None,
+                                      _fptr(q) if q is not None else None))
+
+    def control(self) -> dict:
+        c = AsphControl()
+        _check(self.lib.asph_get_control(self._ctx, C.byref(c)))
+        return {n: getattr(c, n) for n, _ in AsphControl._fields_}
+
+    def set_time(self, simt: float, dt: float = 0.0, do_sort: bool = True) -> None:
+        _check(self.lib.asph_set_time(self._ctx, float(simt), float(dt), int(bool(do_sort))))
+
+    # ---- granular blocks ----------------------------------------------------------
+    def sort_build(self) -> None:
+        _check(self.lib.asph_sort_build(self._ctx))
+
+    def get_sort(self) -> dict:
+        N = self.N
+        kin = np.empty(N, np.uint32)
+        ks = np.empty(N, np.uint32)
+        perm = np.empty(N, np.uint32)
+        rng = np.empty(2 * self.ncell, np.int32)
+        surf = np.empty(N, np.int32)
+        cnt = C.c_int32()
+        u32 = C.POINTER(C.c_uint32)
+        i32 = C.POINTER(C.c_int32)
+        _check(self.lib.asph_get_sort(self._ctx, kin.ctypes.data_as(u32), ks.ctypes.data_as(u32),
+                                      perm.ctypes.data_as(u32), rng.ctypes.data_as(i32),
+                                      surf.ctypes.data_as(i32), C.byref(cnt)))
+        return {"keys_in": kin, "keys_sorted": ks, "perm": perm, "cell_range": rng.reshape(-1, 2),
+                "surf_list": surf[:cnt.value].copy(), "surf_count": cnt.value}
+
+    def kick_drift_flux(self) -> None:
+        _check(self.lib.asph_kick_drift_flux(self._ctx))
+
+    def density_eos(self) -> None:
+        _check(self.lib.asph_density_eos(self._ctx))
+
+    def momentum(self, integrate: bool = True) -> None:
+        _check(self.lib.asph_momentum(self._ctx, int(bool(integrate))))
+
+    def rain(self) -> None:
+        _check(self.lib.asph_rain(self._ctx))
+
+    def cfl(self) -> None:
+        _check(self.lib.asph_cfl(self._ctx))
+
+    # ---- fused step --------------------------------------------------------------------
+    def step(self, nsteps: int = 1) -> None:
+        _check(self.lib.asph_step(self._ctx, int(nsteps)))
+
+    def step_async(self, nsteps: int = 1) -> None:
+        _check(self.lib.asph_step_async(self._ctx, int(nsteps)))
+
+    def step_profiled(self, nsteps: int = 1) -> dict:
+        """Per-phase device milliseconds summed over nsteps (non-graph launches)."""
+        out = np.zeros(abi.NPHASES, np.float32)
+        _check(self.lib.asph_step_profiled(self._ctx, int(nsteps), _fptr(out)))
+        return dict(zip(abi.PHASES, out.tolist()))
+
+    def sync(self) -> None:
+        _check(self.lib.asph_sync(self._ctx))
+
+    # ---- diagnostics ---------------------------------------------------------------------
+    def audit(self) -> np.ndarray:
+        out = np.zeros(6, np.float64)
+        _check(self.lib.asph_audit(self._ctx, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def dump(self, outdir: str) -> str:
+        buf = C.create_string_buffer(1024)
+        os.makedirs(outdir, exist_ok=True)
+        _check(self.lib.asph_dump(self._ctx, outdir.encode(), buf, 1024))
+        return buf.value.decode()
+
+    def column_diag(self) -> dict:
+        out = np.zeros(4, np.float32)
+        _check(self.lib.asph_column_diag(self._ctx, _fptr(out)))
+        return {"cloud_pct": float(out[0]), "ql_max": float(out[1]), "w_max": float(out[2]),
+                "precip_mm": float(out[3])}

@@ -1,0 +1,88 @@
+// asph_internal.cuh — device-side control block, buffer sets and the
+// launch functions shared by the kernel files and the C-ABI layer.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "asph_phys.cuh"
+
+namespace asph {
+
+constexpr int TPB = 256;
+constexpr int SORT_TPB = 256;
+constexpr int SORT_ITEMS = 16;
+constexpr int SORT_TILE = SORT_TPB * SORT_ITEMS;   // keys per radix tile
+constexpr int MAX_PASSES = 4;                      // 30-bit keys / 8-bit digits
+constexpr unsigned SPIN_LIMIT = 1u << 24;          // bounded device waits
+
+// Device-resident step control: the host variables of the reference step
+// loop (asph_h100.cu:931-942, 1040-1078) live here so that a step needs no
+// host round trip.
+struct DevCtl {
+    double simt, since_sort;
+    float dt, dt_required, sort_dt;
+    float umax, vmax, wmax;
+    int step, trips, sort_count, aborted, clamp_pending, do_sort, error, surf_count;
+    int sorted_this_step;
+    unsigned gmax[3];          // float bits of |u|,|v|,|w| maxima (atomicMax)
+    unsigned done;             // finished-block counter of the momentum pass
+    unsigned epoch;            // radix look-back epoch
+    unsigned hist[MAX_PASSES][256];
+    unsigned tile_ctr[MAX_PASSES];
+};
+
+// Buffers of one context.  Particle buffers hold 16-byte field groups.
+struct Bufs {
+    float4* pos[2];     // x, y, z, rho_old (rho gathered for the density pass)
+    float4* vel[2];     // u, v, w, -
+    float4* thq[2];     // theta, qv, qc, -
+    float2* rp;         // rho_new, p'
+    float4* acc;        // ax, ay, az, -
+    float*  dthdt;
+    uint32_t* kin;      // keys of the current order (input of the next sort)
+    uint32_t* kbuf[2];  // radix ping-pong keys
+    uint32_t* vbuf[2];  // radix ping-pong values
+    uint32_t* skeys;    // sorted keys of the last sort (points into kbuf)
+    uint32_t* perm;     // permutation of the last sort (points into vbuf)
+    uint64_t* status;   // look-back words [pass][tile][digit]
+    int2*   range;      // cell table, {start,end}, {0,0} when empty
+    uint8_t* surf;      // 1 when the particle was in the lowest layer at the last sort
+    float*  rain[2];    // Eulerian rain mass per cell [kg]
+    float*  rain_delta; // this step's deposits when the microphysics reads the grid
+    float*  precip;     // accumulated surface precipitation [kg/m^2]
+    DevCtl* ctl;
+    int ntiles, npasses;
+    int pc, vc, qc, rc; // current index of pos/vel/thq/rain ping-pong pairs
+};
+
+// Mode bits of the gather/integrate pass.
+enum : int {
+    G_SORTED    = 1,    // gather through the permutation when a sort ran
+    G_INTEGRATE = 2,    // half kick + drift + surface flux
+    G_FORCE     = 4,    // the sort ran unconditionally (granular call)
+};
+// Mode bits of the momentum pass.
+enum : int {
+    M_INTEGRATE = 1,    // theta update, second half kick, sponge, velocity maxima
+    M_RAIN      = 2,    // rain sedimentation blocks appended to the grid
+    M_CFL       = 4,    // last block runs the CFL control
+};
+
+// ---- launch functions (asph_kernels.cu / asph_sort.cu) --------------------
+void launch_init(const Phys& P, const Bufs& B, const float* bub, int nbub, int init_mode,
+                 int lat_nx, int lat_ny, int lat_nz, float jitter, uint32_t seed, float noise,
+                 cudaStream_t s);
+void launch_keys(const Phys& P, const Bufs& B, cudaStream_t s);
+void launch_sort_prep(const Phys& P, const Bufs& B, int force, int clear_delta, cudaStream_t s);
+void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s);
+void launch_gather(const Phys& P, const Bufs& B, int mode, cudaStream_t s);
+void launch_density(const Phys& P, const Bufs& B, cudaStream_t s);
+void launch_momentum(const Phys& P, const Bufs& B, int mode, cudaStream_t s);
+void launch_rain(const Phys& P, const Bufs& B, cudaStream_t s);
+void launch_cfl(const Phys& P, const Bufs& B, cudaStream_t s);
+void launch_clamp(const Phys& P, const Bufs& B, cudaStream_t s);
+void launch_audit(const Phys& P, const Bufs& B, double* partial, int nblk, double* out, cudaStream_t s);
+void launch_surf_flags(const Phys& P, const Bufs& B, uint8_t* flags, cudaStream_t s);
+void launch_coarse(const Phys& P, const Bufs& B, float* out, int sx, int sy, int sz, int cx, int cy,
+                   int cz, float4* coldiag, cudaStream_t s);
+
+}  // namespace asph

@@ -1,0 +1,69 @@
+"""Test configuration: the `gpu` marker, GPU detection and build-on-demand.
+
+Tests marked `gpu` need a GB300 and call the CUDA path through the C ABI;
+everything else runs on the CPU (oracle, host logic, ABI/export checks).
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def _gpu_count() -> int:
+    try:
+        cu = ctypes.CDLL("libcuda.so.1")
+    except OSError:
+        return 0
+    if cu.cuInit(0) != 0:
+        return 0
+    n = ctypes.c_int(0)
+    if cu.cuDeviceGetCount(ctypes.byref(n)) != 0:
+        return 0
+    return n.value
+
+
+HAVE_GPU = _gpu_count() > 0
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a GB300 GPU (runs the CUDA path through the C ABI)")
+
+
+def pytest_collection_modifyitems(config, items):
+    if HAVE_GPU:
+        return
+    skip = pytest.mark.skip(reason="no CUDA device on this machine")
+    for it in items:
+        if "gpu" in it.keywords:
+            it.add_marker(skip)
+
+
+@pytest.fixture(scope="session", autouse=True)
+def _built():
+    from sph_cuda_gb300 import _build
+    from oracle import build_oracle
+    _build.build_library()
+    build_oracle.build_oracle()
+    yield
+
+
+def golden(name):
+    path = os.path.join(GOLDEN, name)
+    if not os.path.exists(path):
+        pytest.skip("fixture %s not generated" % name)
+    return np.load(path)
+
+
+def normwise(a, b):
+    """||a-b||_inf / ||b||_inf (b is the reference side)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.max(np.abs(b)) if b.size else 0.0
+    num = np.max(np.abs(a - b)) if b.size else 0.0
+    return num / den if den > 0 else num

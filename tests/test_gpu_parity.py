@@ -1,0 +1,342 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the
+reference's own kernels.
+
+Bit-exact: Morton keys, the sorted permutation, sorted keys, cell table,
+surface list, gathered fields.  Floating point: single-stage results agree
+with the FP64 oracle to a normwise relative error of 1e-5
+(||gpu - oracle||_inf / ||oracle||_inf per field), the benchmark spec's bound.
+Each stage of the oracle is fed the GPU's own output of the previous stage,
+so that both sides search identical cell windows.
+"""
+import numpy as np
+import pytest
+
+from sph_cuda_gb300 import Asph, AsphError, abi
+from oracle import oracle
+from conftest import golden, normwise
+from statebuild import small_config, reference_geometry, random_state, as64
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+SORT_FIELDS = ("x", "y", "z", "u", "v", "w", "th", "qv", "qc", "rho")
+
+
+def _case(name):
+    if name == "ref_jitter":
+        return reference_geometry(12, 12, 10), random_state(reference_geometry(12, 12, 10), 1, "jitter")
+    if name == "ref_cluster":
+        p = reference_geometry(10, 12, 8)
+        return p, random_state(p, 3, "cluster")
+    if name == "cfg_jitter":
+        p = small_config()
+        return p, random_state(p, 2, "jitter")
+    if name == "cfg_uniform":
+        p = small_config(beta_av=0.5)
+        return p, random_state(p, 5, "uniform")
+    if name == "cfg_onecell":
+        p = small_config(lat=(5, 4, 3))
+        return p, random_state(p, 4, "onecell")
+    if name == "single":
+        p = small_config(lat=(1, 1, 1))
+        return p, random_state(p, 6, "uniform")
+    raise ValueError(name)
+
+
+def _edges():
+    p = small_config(lat=(4, 4, 4))
+    s = random_state(p, 7, "uniform")
+    Lx, Ly, Lz = np.float32(p.nx * p.dx), np.float32(p.ny * p.dy), np.float32(p.nz * p.dz)
+    s["x"][:6] = [0.0, np.nextafter(Lx, 0, dtype=np.float32), p.dx, np.float32(2 * p.dx) - np.float32(1e-3), 1e-30, Lx / 2]
+    s["y"][:6] = [np.nextafter(Ly, 0, dtype=np.float32), 0.0, p.dy * 3, 1e-3, p.dy, Ly / 3]
+    s["z"][:6] = [Lz, 0.0, p.dz, np.nextafter(np.float32(p.dz), 0, dtype=np.float32), 1e-30, Lz]
+    return p, s
+
+
+def _ctx(p, s, rain=None):
+    sim = Asph(p)
+    sim.set_state(s)
+    if rain is not None:
+        sim.set_rain(rain)
+    return sim
+
+
+def _check_sort(p, s):
+    sim = _ctx(p, s)
+    k0 = sim.get_sort()["keys_in"]
+    assert np.array_equal(k0, oracle.keys(p, s["x"], s["y"], s["z"]))
+    sim.sort_build()
+    gs = sim.get_sort()
+    st = sim.get_state(SORT_FIELDS)
+    ob = oracle.sort_build(p, {k: s[k] for k in SORT_FIELDS})
+    assert np.array_equal(gs["perm"], ob["perm"])
+    assert np.array_equal(gs["keys_sorted"], ob["keys_sorted"])
+    assert np.array_equal(gs["cell_range"], ob["cell_range"])
+    assert np.array_equal(gs["surf_list"], np.nonzero(ob["surf"])[0])
+    for k in SORT_FIELDS:
+        assert np.array_equal(st[k], np.asarray(ob["gathered"][k], np.float32)), k
+    sim.close()
+
+
+@pytest.mark.parametrize("name", ["ref_jitter", "ref_cluster", "cfg_jitter", "cfg_uniform", "cfg_onecell", "single"])
+def test_sort_bit_exact(name):
+    _check_sort(*_case(name))
+
+
+def test_sort_edges_bit_exact():
+    _check_sort(*_edges())
+
+
+def test_sort_sorted_and_reversed_input():
+    p, s = _case("cfg_jitter")
+    ob = oracle.sort_build(p, {k: s[k] for k in SORT_FIELDS})
+    srt = {k: np.asarray(v, np.float32) for k, v in ob["gathered"].items()}
+    _check_sort(p, srt)
+    rev = {k: v[::-1].copy() for k, v in srt.items()}
+    _check_sort(p, rev)
+
+
+def test_sort_full_size_cfg1_bit_exact():
+    p = small_config()
+    from sph_cuda_gb300 import preset
+    p = preset("cfg1")
+    s = random_state(p, 11, "uniform")
+    _check_sort(p, s)
+
+
+def _stages(p, s, simt=1500.0):
+    """Run sort -> kick/drift/flux -> density/EOS -> momentum -> rain -> CFL
+    on the GPU, checking each stage against the oracle fed the GPU's
+    previous-stage output."""
+    rng = np.random.default_rng(9)
+    C = p.nx * p.ny * p.nz
+    rain0 = np.where(rng.uniform(size=C) < .3, rng.uniform(0, 3e4, C), 0.0).astype(np.float32)
+    sim = _ctx(p, s, rain0)
+    sim.sort_build()
+    ctl = sim.control()
+    dt = float(np.float32(ctl["dt_cap"]))
+    sim.set_time(simt, dt, True)
+    g = sim.get_state()
+    srt = sim.get_sort()
+    surf = np.zeros(p.n_particles, np.uint8)
+    surf[srt["surf_list"]] = 1
+    # kick + drift + flux
+    kin = as64(g)
+    if not p.permute_acc:   # the reference kicks with acc in its pre-sort order
+        for k in ("ax", "ay", "az"):
+            kin[k] = np.asarray(s[k], np.float64)
+    sim.kick_drift_flux()
+    kd = sim.get_state()
+    okd = oracle.kick_drift_flux(p, kin, simt, dt, surf)
+    for k in ("x", "y", "z", "u", "v", "w", "th", "qv"):
+        assert normwise(kd[k], okd[k]) < 1e-6, ("kick_drift_flux", k, normwise(kd[k], okd[k]))
+    # density + EOS + microphysics (the table is the pre-drift one)
+    sim.density_eos()
+    de = sim.get_state()
+    ode = oracle.density_eos(p, as64(kd), kd["rho"], srt["cell_range"], dt, rain0)
+    for k, ok in (("rho", "rho"), ("prs", "prs"), ("th", "th"), ("qv", "qv"), ("qc", "qc")):
+        assert normwise(de[k], ode[ok]) < TOL, ("density_eos", k, normwise(de[k], ode[ok]))
+    # momentum + theta update + second kick + sponge
+    sim.momentum(True)
+    mo = sim.get_state()
+    omo = oracle.momentum(p, as64(de), srt["cell_range"], dt, integrate=True)
+    for k in ("ax", "ay", "az", "dthdt", "th", "u", "v", "w"):
+        assert normwise(mo[k], omo[k]) < TOL, ("momentum", k, normwise(mo[k], omo[k]))
+    # rain sedimentation (deposits of this step included)
+    sim.rain()
+    rain, precip = sim.get_rain()
+    reads = p.accretion or p.rain_evap
+    orr, opr = oracle.rain(p, rain0 if reads else rain0 + ode["rain_dep"], dt,
+                           delta=ode["rain_dep"] if reads else None)
+    assert normwise(rain, orr) < TOL
+    assert normwise(precip, opr) < TOL
+    # CFL control from the final velocities
+    sim.cfl()
+    c = sim.control()
+    um = [np.abs(mo[k]).max() for k in ("u", "v", "w")]
+    oc = oracle.cfl(p, um, dt, 0)
+    assert np.allclose([c["umax"], c["vmax"], c["wmax"]], um, rtol=0, atol=0)
+    assert c["dt"] == pytest.approx(oc["dt"], rel=1e-6)
+    assert c["sort_dt"] == pytest.approx(oc["sort_dt"], rel=1e-6)
+    assert c["simt"] == pytest.approx(simt + dt, rel=1e-12)
+    sim.close()
+
+
+@pytest.mark.parametrize("name", ["ref_jitter", "ref_cluster", "cfg_jitter", "cfg_uniform"])
+def test_stages_match_oracle(name):
+    _stages(*_case(name))
+
+
+# ---------------------------------------------------------------------------
+# against the reference's own kernels (fixtures made by running them)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("case", ["jitter", "cluster"])
+def test_stages_match_reference_kernels(case):
+    g = golden("ref_stages_%s.npz" % case)
+    p = reference_geometry(int(g["in_nx"]), int(g["in_ny"]), int(g["in_nz"]))
+    dt, simt = float(g["in_dt"]), float(g["in_simt"])
+    s = {k: g["in_" + k] for k in ("x", "y", "z", "u", "v", "w", "th", "qv", "qc", "rho", "ax", "ay", "az")}
+    sim = _ctx(p, s, g["in_rain"])
+    assert np.array_equal(sim.get_sort()["keys_in"], g["out_keys_in"])
+    sim.sort_build()
+    gs = sim.get_sort()
+    assert np.array_equal(gs["perm"], g["out_perm"])
+    assert np.array_equal(gs["keys_sorted"], g["out_keys_sorted"])
+    assert np.array_equal(gs["cell_range"], g["out_cell_range"])
+    assert np.array_equal(gs["surf_list"], g["out_surf_list"])
+    st = sim.get_state()
+    for k, c in (("x", 0), ("y", 1), ("z", 2)):
+        assert np.array_equal(st[k], g["out_g_pos"][:, c])
+    assert np.array_equal(st["th"], g["out_g_thq"][:, 0])
+    assert np.array_equal(st["rho"], g["out_g_rho"])
+    sim.set_time(simt, dt, True)
+    sim.kick_drift_flux()
+    kd = sim.get_state()
+    for k, c in (("x", 0), ("y", 1), ("z", 2)):
+        assert normwise(kd[k], g["out_kd_pos"][:, c]) < 1e-6
+    for k, c in (("u", 0), ("v", 1), ("w", 2)):
+        assert normwise(kd[k], g["out_kd_vel"][:, c]) < 1e-6
+    for k, c in (("th", 0), ("qv", 1)):
+        assert normwise(kd[k], g["out_flux_thq"][:, c]) < 1e-6
+    # density + EOS from the reference's post-drift state
+    pos, vel, fth = g["out_kd_pos"], g["out_kd_vel"], g["out_flux_thq"]
+    sim.set_state(dict(x=pos[:, 0], y=pos[:, 1], z=pos[:, 2], u=vel[:, 0], v=vel[:, 1], w=vel[:, 2],
+                       th=fth[:, 0], qv=fth[:, 1], qc=fth[:, 2], rho=g["out_g_rho"]))
+    sim.set_rain(g["in_rain"])
+    sim.density_eos()
+    de = sim.get_state()
+    assert normwise(de["rho"], g["out_d_rho"]) < TOL
+    assert normwise(de["prs"], g["out_e_prs"]) < TOL
+    for k, c in (("th", 0), ("qv", 1), ("qc", 2)):
+        assert normwise(de[k], g["out_e_thq"][:, c]) < TOL, k
+    rain, _ = sim.get_rain()
+    assert normwise(rain, g["out_e_rain"]) < TOL
+    # momentum + integrate from the reference's post-EOS state
+    eth = g["out_e_thq"]
+    sim.set_state(dict(x=pos[:, 0], y=pos[:, 1], z=pos[:, 2], u=vel[:, 0], v=vel[:, 1], w=vel[:, 2],
+                       th=eth[:, 0], qv=eth[:, 1], qc=eth[:, 2], rho=g["out_d_rho"], prs=g["out_e_prs"]))
+    sim.momentum(True)
+    mo = sim.get_state()
+    for k, c in (("ax", 0), ("ay", 1), ("az", 2)):
+        assert normwise(mo[k], g["out_m_acc"][:, c]) < TOL, k
+    assert normwise(mo["dthdt"], g["out_m_dthdt"]) < TOL
+    assert normwise(mo["th"], g["out_i_thq"][:, 0]) < TOL
+    for k, c in (("u", 0), ("v", 1), ("w", 2)):
+        assert normwise(mo[k], g["out_i_vel"][:, c]) < TOL, k
+    sim.set_rain(g["out_e_rain"], np.zeros(p.nx * p.ny, np.float32))
+    sim.rain()
+    rain, precip = sim.get_rain()
+    assert normwise(rain, g["out_r_rain"]) < 1e-6
+    assert normwise(precip, g["out_r_precip"]) < 1e-6
+    sim.close()
+
+
+def test_init_matches_reference_kernels():
+    g = golden("ref_init.npz")
+    p = reference_geometry(int(g["nx"]), int(g["ny"]), int(g["nz"]), noise=float(g["noise"]))
+    sim = Asph(p)
+    sim.init()
+    st = sim.get_state()
+    gs = sim.get_sort()
+    assert np.array_equal(gs["perm"], g["perm"])
+    assert np.array_equal(gs["cell_range"], g["cell_range"])
+    for k, c in (("x", 0), ("y", 1), ("z", 2)):
+        assert np.array_equal(st[k], g["pos"][:, c])
+    assert normwise(st["th"], g["thq"][:, 0]) < TOL
+    assert normwise(st["qv"], g["thq"][:, 1]) < TOL
+    assert normwise(st["rho"], g["rho"]) < TOL
+    assert normwise(st["az"], g["acc"][:, 2]) < TOL
+    sim.close()
+
+
+# ---------------------------------------------------------------------------
+# the fused, graph-captured step
+# ---------------------------------------------------------------------------
+def test_graph_step_equals_granular_blocks():
+    p, s = _case("ref_jitter")
+    a = _ctx(p, s)
+    b = _ctx(p, s)
+    a.step(1)
+    b.sort_build(); b.kick_drift_flux(); b.density_eos(); b.momentum(True); b.rain(); b.cfl()
+    sa, sb = a.get_state(), b.get_state()
+    for k in ("x", "y", "z", "u", "v", "w", "th", "qv", "qc", "rho", "ax", "ay", "az", "prs", "dthdt"):
+        assert np.array_equal(sa[k], sb[k]), k
+    ca, cb = a.control(), b.control()
+    for k in ("dt", "simt", "sort_dt", "umax", "wmax", "step"):
+        assert ca[k] == cb[k], k
+    ra, rb = a.get_rain()[0], b.get_rain()[0]
+    assert normwise(ra, rb) < 1e-6
+
+
+def test_steps_deterministic_and_conserve_water():
+    p = small_config(lat=(16, 16, 16), accretion=0, rain_evap=0, surface_flux=0, sort_every=1)
+    sims = []
+    for _ in range(2):
+        sim = Asph(p)
+        sim.init()
+        sims.append(sim)
+    a0 = sims[0].audit()
+    r0 = sims[0].get_rain()[0].astype(np.float64).sum()
+    for sim in sims:
+        sim.step(30)
+    s0, s1 = sims[0].get_state(), sims[1].get_state()
+    for k in ("x", "z", "w", "th", "qc"):
+        assert np.array_equal(s0[k], s1[k]), k
+    a1 = sims[0].audit()
+    rain, precip = sims[0].get_rain()
+    water0 = a0[3] + r0
+    water1 = a1[3] + rain.astype(np.float64).sum() + precip.astype(np.float64).sum() * p.dx * p.dy
+    assert abs(water1 / water0 - 1) < 1e-5
+    assert abs(a1[5] / a0[5] - 1) < 1e-12
+    c = sims[0].control()
+    assert c["step"] == 30 and c["sort_count"] >= 30
+
+
+def test_cfl_trip_clamps_and_strict_aborts():
+    p = reference_geometry(16, 16, 8)
+    s = random_state(p, 8, "jitter", speed=300.0)
+    sim = _ctx(p, s)
+    sim.step(1)
+    c = sim.control()
+    assert c["trips"] == 1 and c["clamp_pending"] == 1
+    st = sim.get_state()
+    sp = np.sqrt(st["u"].astype(np.float64) ** 2 + st["v"] ** 2 + st["w"] ** 2)
+    assert sp.max() <= 0.5 * p.cs * (1 + 1e-6)
+    ps = reference_geometry(16, 16, 8, strict_cfl=1)
+    sim2 = _ctx(ps, s)
+    with pytest.raises(AsphError) as e:
+        sim2.step(3)
+    assert e.value.status == abi.ASPH_ERR_CFL_ABORT
+    c2 = sim2.control()
+    assert c2["aborted"] == 1 and c2["step"] == 0
+    frozen = sim2.get_state()
+    with pytest.raises(AsphError):
+        sim2.step(2)
+    again = sim2.get_state()
+    assert np.array_equal(frozen["x"], again["x"])
+
+
+def test_dump_matches_host_means(tmp_path):
+    from sph_cuda_gb300 import dumpfmt
+    p = reference_geometry(20, 20, 9)
+    sim = Asph(p)
+    sim.init()
+    sim.step(3)
+    path = sim.dump(str(tmp_path))
+    d = dumpfmt.read(path)
+    c = sim.control()
+    assert path.endswith("asph_t%06.0fs.bin" % c["simt"])
+    assert (d["nx"], d["ny"], d["nz"], d["sx"], d["sy"], d["sz"]) == (20, 20, 9, 10, 10, 3)
+    assert d["dt"] == pytest.approx(c["dt"])
+    st = sim.get_state()
+    rng = sim.get_sort()["cell_range"]
+    means = np.zeros((d["cz"], d["cy"], d["cx"], 6))
+    cnt = np.zeros((d["cz"], d["cy"], d["cx"]))
+    for cid in range(p.nx * p.ny * p.nz):
+        ix, iy, iz = cid % p.nx, (cid // p.nx) % p.ny, cid // (p.nx * p.ny)
+        a, b = rng[cid]
+        for j in range(a, b):
+            means[iz // 3, iy // 10, ix // 10] += [st["th"][j], st["qv"][j], st["qc"][j], st["u"][j], st["v"][j],
+                                                   st["w"][j]]
+            cnt[iz // 3, iy // 10, ix // 10] += 1
+    means /= np.maximum(cnt, 1)[..., None]
+    assert np.allclose(d["data"], means, rtol=1e-5, atol=1e-6)
