@@ -208,6 +208,15 @@ int asph_sync(asph_ctx* ctx);
 #define ASPH_NPHASES 6
 int asph_step_profiled(asph_ctx* ctx, int nsteps, float* phase_ms);
 
+/* Execution options.  ASPH_OPT_PAIR_PATH: 0 = automatic (brick-staged
+ * shared-memory pair kernels where the grid allows), 1 = per-target global
+ * path everywhere (same results; for testing).  ASPH_OPT_PAIR_SHAPE (get
+ * only): index of the brick shape in use, -1 for the global path. */
+#define ASPH_OPT_PAIR_PATH  1
+#define ASPH_OPT_PAIR_SHAPE 2
+int asph_set_option(asph_ctx* ctx, int option, int value);
+int asph_get_option(asph_ctx* ctx, int option, int* value);
+
 /* ---- diagnostics and output ----------------------------------------------- */
 /* FP64 totals: KE, PE, IE, water, p_z, mass (asph_h100.cu:650-668). */
 int asph_audit(asph_ctx* ctx, double out[6]);

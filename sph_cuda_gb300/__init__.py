@@ -189,6 +189,15 @@ class Asph:
         _check(self.lib.asph_step_profiled(self._ctx, int(nsteps), _fptr(out)))
         return dict(zip(abi.PHASES, out.tolist()))
 
+    def set_pair_path(self, global_path: bool) -> None:
+        """Force the per-target global pair path (True) or automatic (False)."""
+        _check(self.lib.asph_set_option(self._ctx, abi.OPT_PAIR_PATH, int(bool(global_path))))
+
+    def pair_shape(self) -> int:
+        v = C.c_int()
+        _check(self.lib.asph_get_option(self._ctx, abi.OPT_PAIR_SHAPE, C.byref(v)))
+        return v.value
+
     def sync(self) -> None:
         _check(self.lib.asph_sync(self._ctx))
 

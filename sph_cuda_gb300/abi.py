@@ -26,6 +26,8 @@ QV_REFERENCE = 0
 QV_RH = 1
 MAX_BUBBLES = 8
 NPHASES = 6
+OPT_PAIR_PATH = 1
+OPT_PAIR_SHAPE = 2
 PHASES = ("table_clear", "sort", "gather_kick_drift", "density_eos", "momentum_integrate", "step")
 
 _f = C.c_float
@@ -119,6 +121,8 @@ SIGNATURES = {
     "asph_step_async": (C.c_int, [_P, C.c_int]),
     "asph_sync": (C.c_int, [_P]),
     "asph_step_profiled": (C.c_int, [_P, C.c_int, _FP]),
+    "asph_set_option": (C.c_int, [_P, C.c_int, C.c_int]),
+    "asph_get_option": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int)]),
     "asph_audit": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "asph_dump": (C.c_int, [_P, C.c_char_p, C.c_char_p, C.c_int]),
     "asph_column_diag": (C.c_int, [_P, _FP]),

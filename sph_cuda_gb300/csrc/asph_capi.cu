@@ -56,6 +56,7 @@ struct asph_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool initialised = false;
+    bool lists_valid = false;   // neighbour lists match the current positions
     // graphs keyed by the ping-pong state at the start of the step
     cudaGraphExec_t gexec[16] = {};
     // staging for host <-> device SoA copies (16 floats per particle)
@@ -220,6 +221,9 @@ extern "C" int asph_params_check(const AsphParams* p) {
     if (p->n_bubbles < 0 || p->n_bubbles > ASPH_MAX_BUBBLES) return fail(ASPH_ERR_CONFIG, "n_bubbles out of range");
     if (!(p->cs > 0.f) || !(p->cfl > 0.f)) return fail(ASPH_ERR_CONFIG, "cs and cfl must be positive");
     if (p->dump_sx < 1 || p->dump_sy < 1 || p->dump_sz < 1) return fail(ASPH_ERR_CONFIG, "dump strides must be >= 1");
+    if (p->qv_mode == ASPH_QV_RH && p->z_bl != floorf(p->z_bl))
+        return fail(ASPH_ERR_CONFIG, "z_bl must be a whole number of metres (sounding table node spacing)");
+    if (!(p->nz * p->dz < 60000.f)) return fail(ASPH_ERR_CONFIG, "domain top must be below 60 km");
     return ASPH_OK;
 }
 
@@ -258,6 +262,70 @@ static void derive(const AsphParams& p, Phys& P) {
     P.sort_every = p.sort_every; P.permute_acc = p.permute_acc;
     const int nmax = p.nx > p.ny ? (p.nx > p.nz ? p.nx : p.nz) : (p.ny > p.nz ? p.ny : p.nz);
     P.key_bits = 3 * ceil_log2(nmax);
+}
+
+// Reference sounding in double (asph_h100.cu:136-153, 155-163) for the
+// device tables.  One node per metre of height; on [k, k+1) the value is a
+// quadratic through the values at k, k+1/2 and k+1 (left limit), stored as
+// {hi, lo, c1, c2} so that the device recovers the value as the pair
+// hi + (lo + t (c1 + t c2)) to ~1e-11 relative.
+namespace {
+struct SndD {
+    double th0, n2, a;
+    int qv_mode;
+    double qv0, rh, rh_bl, z_bl;
+};
+constexpr double G_D = 9.80665, RD_D = 287.05, CP_D = 1004.0, P0_D = 100000.0;
+double th_ref_d(const SndD& s, double z) { return s.th0 * exp(s.n2 * z / G_D); }
+double ex_ref_d(const SndD& s, double z) { return 1.0 - s.a * (1.0 - exp(-s.n2 * z / G_D)); }
+double p_ref_d(const SndD& s, double z) { return P0_D * pow(ex_ref_d(s, z), CP_D / RD_D); }
+double rho_ref_d(const SndD& s, double z) { return p_ref_d(s, z) / (RD_D * th_ref_d(s, z) * ex_ref_d(s, z)); }
+double esat_d(double T) {
+    const double Tc = T - 273.15;
+    return 611.2 * exp(17.67 * Tc / (Tc + 243.5));
+}
+double qsat_d(double T, double p) {
+    const double es = fmin(esat_d(T), 0.5 * p);
+    const double den = p - 0.378 * es;
+    return den > 1.0 ? 0.622 * es / den : 0.0;
+}
+double qv_ref_d(const SndD& s, double z) {
+    if (s.qv_mode == ASPH_QV_REFERENCE) return s.qv0 * exp(-z / 2500.0) * exp(-fmax(z - 5000.0, 0.0) / 1000.0);
+    const double ex = ex_ref_d(s, z);
+    return (z < s.z_bl ? s.rh_bl : s.rh) * qsat_d(th_ref_d(s, z) * ex, P0_D * pow(ex, CP_D / RD_D));
+}
+double thvr_d(const SndD& s, double z) { return th_ref_d(s, z) * (1.0 + 0.608 * qv_ref_d(s, z)); }
+
+template <class F>
+void fill_table(float4* out, int n, F&& f) {
+    for (int k = 0; k < n; ++k) {
+        const double f0 = f((double)k), fm = f(k + 0.5), f1 = f(k + 1.0 - 1e-9);
+        const float hi = (float)f0;
+        out[k] = make_float4(hi, (float)(f0 - (double)hi), (float)(-3.0 * f0 + 4.0 * fm - f1),
+                             (float)(2.0 * f0 - 4.0 * fm + 2.0 * f1));
+    }
+}
+}  // namespace
+
+static int build_sounding(asph_ctx* c) {
+    const AsphParams& p = c->prm;
+    SndD s;
+    s.th0 = p.th0; s.n2 = p.n2;
+    s.a = G_D * G_D / (CP_D * s.th0 * s.n2);
+    s.qv_mode = p.qv_mode; s.qv0 = p.qv0; s.rh = p.rh; s.rh_bl = p.rh_bl; s.z_bl = p.z_bl;
+    const int n = (int)ceil((double)c->P.lz) + 2;
+    std::vector<float4> h((size_t)3 * n);
+    fill_table(h.data(), n, [&](double z) { return rho_ref_d(s, z); });
+    fill_table(h.data() + n, n, [&](double z) { return p_ref_d(s, z); });
+    fill_table(h.data() + 2 * n, n, [&](double z) { return thvr_d(s, z); });
+    CKR(c->alloc(&c->B.snd, h.size() * sizeof(float4)));
+    CKR(cudaMemcpyAsync(c->B.snd, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    CKR(cudaStreamSynchronize(c->stream));
+    c->P.snd_rho = c->B.snd;
+    c->P.snd_p = c->B.snd + n;
+    c->P.snd_thvr = c->B.snd + 2 * n;
+    c->P.snd_n = n;
+    return ASPH_OK;
 }
 
 static int reset_control(asph_ctx* c) {
@@ -309,6 +377,8 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     AL(B.status, (size_t)B.npasses * B.ntiles * 256 * 8);
     AL(B.range, C * 8); AL(B.surf, N); AL(B.rain_delta, C * 4); AL(B.precip, (size_t)P.nxy * 4);
     AL(B.ctl, sizeof(DevCtl));
+    AL(B.nbr, (size_t)NBR_CAP * N * 4);
+    AL(B.nbr_cnt, N * 4);
 #undef AL
     if (e != cudaSuccess) {
         delete c;
@@ -330,11 +400,13 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     if (e == cudaSuccess) e = cudaMemsetAsync(B.surf, 0, N, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.perm, 0, N * 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.skeys, 0, N * 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.nbr_cnt, 0xff, N * 4, s);   // -1: no list yet
     if (e != cudaSuccess) {
         delete c;
         return fail(ASPH_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
     }
-    st = reset_control(c);
+    st = build_sounding(c);
+    if (!st) st = reset_control(c);
     if (st) {
         delete c;
         return st;
@@ -360,6 +432,32 @@ static int sync_status(asph_ctx* c) {
     if (words[1]) return fail(words[1], "device error word %d", words[1]);
     if (words[0]) return fail(ASPH_ERR_CFL_ABORT, "CFL abort: the scheme is outside its stability envelope");
     return ASPH_OK;
+}
+
+extern "C" int asph_set_option(asph_ctx* c, int option, int value) {
+    if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
+    if (option == ASPH_OPT_PAIR_PATH) {
+        if (value < 0 || value > 1) return fail(ASPH_ERR_ARG, "pair path must be 0 (auto) or 1 (global)");
+        c->B.force_global = value;
+    } else {
+        return fail(ASPH_ERR_ARG, "unknown option %d", option);
+    }
+    for (auto& g : c->gexec)   // captured graphs hold the old kernels
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    return ASPH_OK;
+}
+
+extern "C" int asph_get_option(asph_ctx* c, int option, int* value) {
+    if (!c || !value) return fail(ASPH_ERR_ARG, "NULL argument");
+    if (option == ASPH_OPT_PAIR_PATH) {
+        *value = c->B.force_global;
+        return ASPH_OK;
+    }
+    if (option == ASPH_OPT_PAIR_SHAPE) {
+        *value = c->B.force_global ? -1 : pair_shape(c->P);
+        return ASPH_OK;
+    }
+    return fail(ASPH_ERR_ARG, "unknown option %d", option);
 }
 
 extern "C" int asph_sync(asph_ctx* c) {
@@ -398,7 +496,8 @@ extern "C" int asph_init(asph_ctx* c) {
     launch_keys(c->P, c->B, c->stream);
     do_sort_build(c, 1);
     launch_density(c->P, c->B, c->stream);
-    launch_momentum(c->P, c->B, 0, c->stream);
+    launch_momentum(c->P, c->B, 0, 1, c->stream);
+    c->lists_valid = true;
     CKR(cudaGetLastError());
     c->initialised = true;
     return sync_status(c);
@@ -467,6 +566,7 @@ extern "C" int asph_set_state(asph_ctx* c, const AsphHostState* s) {
     launch_keys(c->P, B, c->stream);
     CKR(cudaGetLastError());
     c->initialised = true;
+    c->lists_valid = false;
     return sync_status(c);
 }
 
@@ -563,6 +663,7 @@ extern "C" int asph_sort_build(asph_ctx* c) {
     int st = ensure_stage(c);
     if (st) return st;
     do_sort_build(c, 1);
+    c->lists_valid = false;
     Bufs& B = c->B;
     const int nb = (c->P.N + TPB - 1) / TPB;
     float4* tmp = reinterpret_cast<float4*>(c->stage);
@@ -602,6 +703,7 @@ extern "C" int asph_kick_drift_flux(asph_ctx* c) {
     if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
     launch_gather(c->P, c->B, G_INTEGRATE, c->stream);
     c->B.pc ^= 1; c->B.vc ^= 1; c->B.qc ^= 1;
+    c->lists_valid = false;
     CKR(cudaGetLastError());
     return sync_status(c);
 }
@@ -609,13 +711,14 @@ extern "C" int asph_kick_drift_flux(asph_ctx* c) {
 extern "C" int asph_density_eos(asph_ctx* c) {
     if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
     launch_density(c->P, c->B, c->stream);
+    c->lists_valid = true;
     CKR(cudaGetLastError());
     return sync_status(c);
 }
 
 extern "C" int asph_momentum(asph_ctx* c, int integrate) {
     if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
-    launch_momentum(c->P, c->B, integrate ? M_INTEGRATE : 0, c->stream);
+    launch_momentum(c->P, c->B, integrate ? M_INTEGRATE : 0, c->lists_valid ? 1 : 0, c->stream);
     if (integrate) c->B.vc ^= 1;
     CKR(cudaGetLastError());
     return sync_status(c);
@@ -645,8 +748,9 @@ static void enqueue_step(asph_ctx* c) {
     launch_gather(P, c->B, G_SORTED | G_INTEGRATE, c->stream);
     c->B.pc ^= 1; c->B.vc ^= 1; c->B.qc ^= 1;
     launch_density(P, c->B, c->stream);
-    launch_momentum(P, c->B, M_INTEGRATE | M_RAIN | M_CFL, c->stream);
+    launch_momentum(P, c->B, M_INTEGRATE | M_RAIN | M_CFL, 1, c->stream);
     c->B.vc ^= 1; c->B.rc ^= 1;
+    c->lists_valid = true;
 }
 
 extern "C" int asph_step_profiled(asph_ctx* c, int nsteps, float* phase_ms) {
@@ -669,7 +773,7 @@ extern "C" int asph_step_profiled(asph_ctx* c, int nsteps, float* phase_ms) {
         cudaEventRecord(ev[3], s);
         launch_density(P, c->B, s);
         cudaEventRecord(ev[4], s);
-        launch_momentum(P, c->B, M_INTEGRATE | M_RAIN | M_CFL, s);
+        launch_momentum(P, c->B, M_INTEGRATE | M_RAIN | M_CFL, 1, s);
         c->B.vc ^= 1; c->B.rc ^= 1;
         cudaEventRecord(ev[5], s);
         cudaError_t e = cudaEventSynchronize(ev[5]);
@@ -709,6 +813,7 @@ extern "C" int asph_step_async(asph_ctx* c, int nsteps) {
         }
         CKR(cudaGraphLaunch(c->gexec[slot], c->stream));
         c->B.pc ^= 1; c->B.qc ^= 1; c->B.rc ^= 1;   // vel flips twice per step
+        c->lists_valid = true;
     }
     return ASPH_OK;
 }

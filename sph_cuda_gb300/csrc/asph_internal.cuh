@@ -13,6 +13,7 @@ constexpr int SORT_ITEMS = 16;
 constexpr int SORT_TILE = SORT_TPB * SORT_ITEMS;   // keys per radix tile
 constexpr int MAX_PASSES = 4;                      // 30-bit keys / 8-bit digits
 constexpr unsigned SPIN_LIMIT = 1u << 24;          // bounded device waits
+constexpr int NBR_CAP = 64;                        // neighbour-list slots per particle
 
 // Device-resident step control: the host variables of the reference step
 // loop (asph_h100.cu:931-942, 1040-1078) live here so that a step needs no
@@ -50,8 +51,12 @@ struct Bufs {
     float*  rain_delta; // this step's deposits when the microphysics reads the grid
     float*  precip;     // accumulated surface precipitation [kg/m^2]
     DevCtl* ctl;
+    float4* snd;        // sounding tables: rho_ref, pres_ref, thvr (3 x snd_n nodes)
+    int*    nbr;        // neighbour lists of the density pass, slot-major [NBR_CAP][N]
+    int*    nbr_cnt;    // neighbours per particle, -1 when the list overflowed
     int ntiles, npasses;
     int pc, vc, qc, rc; // current index of pos/vel/thq/rain ping-pong pairs
+    int force_global;   // 1: pair passes take the per-target global path
 };
 
 // Mode bits of the gather/integrate pass.
@@ -76,8 +81,9 @@ void launch_sort_prep(const Phys& P, const Bufs& B, int force, int clear_delta, 
 void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s);
 void launch_gather(const Phys& P, const Bufs& B, int mode, cudaStream_t s);
 void launch_density(const Phys& P, const Bufs& B, cudaStream_t s);
-void launch_momentum(const Phys& P, const Bufs& B, int mode, cudaStream_t s);
+void launch_momentum(const Phys& P, const Bufs& B, int mode, int use_lists, cudaStream_t s);
 void launch_rain(const Phys& P, const Bufs& B, cudaStream_t s);
+int pair_shape(const Phys& P);
 void launch_cfl(const Phys& P, const Bufs& B, cudaStream_t s);
 void launch_clamp(const Phys& P, const Bufs& B, cudaStream_t s);
 void launch_audit(const Phys& P, const Bufs& B, double* partial, int nblk, double* out, cudaStream_t s);

@@ -1,0 +1,553 @@
+// asph_pairs.cu — the two pair passes of the step, for sm_103a:
+//   D  density (lagged Shepard) + EOS + microphysics (asph_h100.cu:286-402)
+//   M  momentum + integration + rain sedimentation + CFL control
+//      (asph_h100.cu:415-599, 1040-1078)
+//
+// Candidate set (identical to the reference): for target i, every particle
+// listed by the cell table in the cells within +-2 of i's *current* cell,
+// x/y wrapped, z clipped at the walls; the table is the one built at the
+// last sort (positions have drifted since), distances are raw coordinate
+// differences in cell units (no minimum image).  D and M see the same
+// positions and table, so they accept the same pairs: D enumerates the
+// candidates once and records each target's accepted neighbours (self
+// excluded) in a slot-major list; M walks that list.
+//
+// D, brick path.  One CTA per Morton-aligned brick of BX x BY x BZ cells;
+// the brick's targets are one contiguous span of the sorted order and the
+// block has about as many threads as a brick has targets.  The CTA copies
+// the particles of every table cell within HALO = 3 cells of the brick
+// (stencil 2 + 1 cell of drift since the sort) into shared memory, bucketed
+// row-major by region cell, so that each row of a target's 5 x 5 x 5 window
+// is one contiguous span of shared memory; each thread walks its target's
+// row spans in one flattened loop, queues accepted candidates in a small
+// per-thread list in shared memory, and drains the list (density sums +
+// neighbour-list writes) in uniform loops.  A target whose window leaves
+// the staged region (drift > 1 cell), or a brick whose region overflows the
+// staging capacity, takes the global path.
+//
+// Global path.  One thread per target walking the cell table in global
+// memory, the reference's loop structure; used for grids narrower than the
+// staged region, for the fallbacks above, and by M for a target whose list
+// overflowed or was not produced on the current positions.
+#include "asph_device.cuh"
+#include "../../include/asph.h"
+
+namespace asph {
+
+constexpr int HALO = 3;
+constexpr int DLIST = 16;        // queued accepted candidates per thread (D)
+constexpr int M_TPB = 256;
+
+template <int BX, int BY, int BZ>
+struct BrickGeom {
+    static_assert((BX == BY && BY == BZ) || (BX == 2 * BY && BY == BZ) || (BX == BY && BX == 2 * BZ),
+                  "brick must be a Morton-aligned key range");
+    static constexpr int RX = BX + 2 * HALO, RY = BY + 2 * HALO, RZ = BZ + 2 * HALO;
+    static constexpr int R = RX * RY * RZ;
+    static constexpr int KEYS = BX * BY * BZ;
+};
+
+struct PairCfg {
+    int nbx, nby, nbz, nbricks;
+    int cap;            // staged particles that fit in shared memory
+};
+
+namespace {
+
+__device__ __forceinline__ int lower_bound_u32(const uint32_t* __restrict__ a, int n, uint32_t key) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&a[mid]) < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// Exclusive scan of one int per thread over the block (any multiple of 32
+// up to 1024 threads).
+__device__ __forceinline__ int block_excl_scan_int(int v, int* s_warp, int* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < nw ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nw) s_warp[lane] = w;
+    }
+    __syncthreads();
+    const int off = warp ? s_warp[warp - 1] : 0;
+    *total = s_warp[nw - 1];
+    __syncthreads();
+    return x - v + off;
+}
+
+// Walk the reference window of one target through the global cell table.
+template <class F>
+__device__ __forceinline__ void for_window_global(const Phys& P, const int2* __restrict__ range, float x, float y,
+                                                  float z, F&& f) {
+    const int ix = cell_ix(x, P.inv_dx, P.nx), iy = cell_ix(y, P.inv_dy, P.ny), iz = cell_ix(z, P.inv_dz, P.nz);
+    const int z0 = max(iz - STENCIL, 0), z1 = min(iz + STENCIL, P.nz - 1);
+    for (int jz = z0; jz <= z1; ++jz)
+        for (int jy = iy - STENCIL; jy <= iy + STENCIL; ++jy) {
+            const int cy = wrapi(jy, P.ny);
+            const int2* row = range + (size_t)(jz * P.ny + cy) * P.nx;
+            for (int jx = ix - STENCIL; jx <= ix + STENCIL; ++jx) {
+                const int2 rg = row[wrapi(jx, P.nx)];
+                for (int j = rg.x; j < rg.y; ++j) f(j);
+            }
+        }
+}
+
+// Region-local window of a target: returns false if it leaves the region.
+template <int BX, int BY, int BZ>
+__device__ __forceinline__ bool local_window(const Phys& P, int bxi, int byi, int bzi, float x, float y, float z,
+                                             int& lx, int& ly, int& zlo, int& zhi) {
+    using G = BrickGeom<BX, BY, BZ>;
+    const int ix = cell_ix(x, P.inv_dx, P.nx), iy = cell_ix(y, P.inv_dy, P.ny), iz = cell_ix(z, P.inv_dz, P.nz);
+    lx = ix - (bxi * BX - HALO);
+    lx += lx < 0 ? P.nx : 0; lx -= lx >= P.nx ? P.nx : 0;
+    ly = iy - (byi * BY - HALO);
+    ly += ly < 0 ? P.ny : 0; ly -= ly >= P.ny ? P.ny : 0;
+    const int rz0 = bzi * BZ - HALO;
+    zlo = max(iz - STENCIL, 0) - rz0;
+    zhi = min(iz + STENCIL, P.nz - 1) - rz0;
+    return lx >= STENCIL && lx < G::RX - STENCIL && ly >= STENCIL && ly < G::RY - STENCIL && zlo >= 0 &&
+           zhi < G::RZ;
+}
+
+// Flattened walk of the 5 x 5 x (z rows) window inside the staged region.
+template <int BX, int BY, int BZ, class F>
+__device__ __forceinline__ void for_window_smem(const int* s_off, int lx, int ly, int zlo, int zhi, F&& f) {
+    using G = BrickGeom<BX, BY, BZ>;
+    int jz = zlo, jy = ly - STENCIL;
+    int la = (jz * G::RY + jy) * G::RX + lx - STENCIL;
+    int k = s_off[la], kend = s_off[la + 5];
+    for (;;) {
+        if (k < kend) {
+            f(k);
+            ++k;
+            continue;
+        }
+        if (++jy > ly + STENCIL) {
+            jy = ly - STENCIL;
+            if (++jz > zhi) break;
+        }
+        la = (jz * G::RY + jy) * G::RX + lx - STENCIL;
+        k = s_off[la];
+        kend = s_off[la + 5];
+    }
+}
+
+__device__ __forceinline__ float r2_cells(const Phys& P, float xi, float yi, float zi, float xj, float yj, float zj) {
+    const float dx = (xi - xj) * P.inv_dx, dy = (yi - yj) * P.inv_dy, dz = (zi - zj) * P.inv_dz;
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// Neighbour-list writer of one target (slot-major, coalesced over targets).
+struct NbrOut {
+    int* nbr;
+    int n, N, i;
+    __device__ __forceinline__ void push(int j) {
+        if (n < NBR_CAP) nbr[(size_t)n * N + i] = j;
+        ++n;
+    }
+};
+
+}  // namespace
+
+// ===========================================================================
+// D: density + EOS + microphysics, neighbour lists
+// ===========================================================================
+struct DArgs {
+    const float4* pos;      // x, y, z, rho_old
+    const int2* range;
+    const uint32_t* skeys;  // sorted keys of the table's order
+    DOut out;
+    int* nbr;
+    int* nbr_cnt;
+    DevCtl* ctl;
+};
+
+// Out of line: only targets that leave the staged region come here, and
+// keeping it out of the brick kernel keeps that kernel free of spills.
+__device__ __noinline__ void density_target_global(const Phys& P, const DArgs& A, int i, float4 pi, DSum& s,
+                                                    const FF& rr) {
+    NbrOut L{A.nbr, 0, P.N, i};
+    for_window_global(P, A.range, pi.x, pi.y, pi.z, [&](int j) {
+        const float4 pj = A.pos[j];
+        const float r2 = r2_cells(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z);
+        if (r2 < 4.0f) {
+            dsum_add(s, r2, pj.w, rr);
+            if (r2 >= 1e-12f) L.push(j);
+        }
+    });
+    A.nbr_cnt[i] = L.n <= NBR_CAP ? L.n : -1;
+}
+
+__global__ __launch_bounds__(256) void k_density_global(const __grid_constant__ Phys P,
+                                                        const __grid_constant__ DArgs A) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (A.ctl->aborted || i >= P.N) return;
+    const float dt = A.ctl->dt;
+    const float4 pi = A.pos[i];
+    const FF rr = snd_eval(P.snd_rho, P.snd_n, pi.z);
+    DSum s{0.f, 0.f, 0.f};
+    density_target_global(P, A, i, pi, s, rr);
+    density_eos_epilogue(P, A.out, i, pi, s, rr, dt);
+}
+
+template <int BX, int BY, int BZ>
+__global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ Phys P, const __grid_constant__ DArgs A,
+                                                       PairCfg C) {
+    using G = BrickGeom<BX, BY, BZ>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int T = blockDim.x;
+    float4* sp = reinterpret_cast<float4*>(smem);                       // x, y, z, rho_old
+    int* s_gidx = reinterpret_cast<int*>(sp + C.cap);                    // global index of a staged slot
+    int* s_off = s_gidx + C.cap;                                         // R + 1
+    int* s_start = s_off + (G::R + 1);                                   // R
+    // the drain queue reuses s_start, which is only needed while staging
+    unsigned short* s_list = reinterpret_cast<unsigned short*>(s_start);      // DLIST x T
+    __shared__ int s_warp[32];
+    __shared__ int s_span[2];
+    if (A.ctl->aborted) return;
+    const int b = blockIdx.x;
+    const int bxi = b % C.nbx, byi = (b / C.nbx) % C.nby, bzi = b / (C.nbx * C.nby);
+    if (threadIdx.x < 2) {
+        const uint32_t base = morton3((uint32_t)(bxi * BX), (uint32_t)(byi * BY), (uint32_t)(bzi * BZ));
+        s_span[threadIdx.x] = lower_bound_u32(A.skeys, P.N, base + (threadIdx.x ? (uint32_t)G::KEYS : 0u));
+    }
+    const float dt = A.ctl->dt;
+
+    // ---- stage the region: counts, scan, copy (row-major by region cell)
+    const int rx0 = bxi * BX - HALO, ry0 = byi * BY - HALO, rz0 = bzi * BZ - HALO;
+    const int chunk = (G::R + T - 1) / T;
+    const int l0 = threadIdx.x * chunk, l1 = min(l0 + chunk, G::R);
+    int run = 0;
+    for (int l = l0; l < l1; ++l) {
+        const int lx = l % G::RX, ly = (l / G::RX) % G::RY, lz = l / (G::RX * G::RY);
+        const int gz = rz0 + lz;
+        int c = 0, st = 0;
+        if (gz >= 0 && gz < P.nz) {
+            int gx = rx0 + lx, gy = ry0 + ly;
+            gx += gx < 0 ? P.nx : 0; gx -= gx >= P.nx ? P.nx : 0;
+            gy += gy < 0 ? P.ny : 0; gy -= gy >= P.ny ? P.ny : 0;
+            const int2 rg = A.range[(size_t)(gz * P.ny + gy) * P.nx + gx];
+            st = rg.x;
+            c = rg.y - rg.x;
+        }
+        s_start[l] = st;
+        s_off[l] = c;
+        run += c;
+    }
+    int total;
+    int excl = block_excl_scan_int(run, s_warp, &total);
+    for (int l = l0; l < l1; ++l) {
+        const int c = s_off[l];
+        s_off[l] = excl;
+        excl += c;
+    }
+    if (threadIdx.x == 0) s_off[G::R] = total;
+    __syncthreads();
+    const bool staged = total <= C.cap;
+    if (staged) {
+        for (int l = l0; l < l1; ++l) {
+            const int o = s_off[l], c = s_off[l + 1] - o, st = s_start[l];
+            for (int k = 0; k < c; ++k) {
+                sp[o + k] = A.pos[st + k];
+                s_gidx[o + k] = st + k;
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- targets, one warp-synchronous round of 32 targets at a time
+    const int ts = s_span[0], te = s_span[1];
+    const int lane = threadIdx.x & 31;
+    for (int base = ts + (threadIdx.x & ~31); base < te; base += T) {
+        const int i = base + lane;
+        const bool active = i < te;
+        float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+        FF rr{0.f, 0.f};
+        DSum s{0.f, 0.f, 0.f};
+        int lx = 0, ly = 0, zlo = 0, zhi = -1;
+        bool fast = false;
+        if (active) {
+            pi = A.pos[i];
+            rr = snd_eval(P.snd_rho, P.snd_n, pi.z);
+            fast = staged && local_window<BX, BY, BZ>(P, bxi, byi, bzi, pi.x, pi.y, pi.z, lx, ly, zlo, zhi);
+        }
+        NbrOut L{A.nbr, 0, P.N, i};
+        int n = 0;
+        // all lanes drain their queues together, in lockstep
+#define ASPH_DRAIN()                                                                  \
+    do {                                                                              \
+        const int nmax_ = __reduce_max_sync(0xffffffffu, n);                          \
+        for (int q = 0; q < nmax_; ++q) {                                             \
+            if (q < n) {                                                              \
+                const int kq = s_list[q * T + threadIdx.x];                           \
+                const float4 pj = sp[kq];                                             \
+                const float r2 = r2_cells(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z);     \
+                dsum_add(s, r2, pj.w, rr);                                            \
+                if (r2 >= 1e-12f) L.push(s_gidx[kq]);                                 \
+            }                                                                         \
+        }                                                                             \
+        n = 0;                                                                        \
+    } while (0)
+        // flattened walk of the window rows in the staged region
+        bool done = !fast;
+        int jz = zlo, jy = ly - STENCIL, k = 0, kend = 0;
+        if (!done) {
+            const int la = (jz * G::RY + jy) * G::RX + lx - STENCIL;
+            k = s_off[la];
+            kend = s_off[la + 5];
+        }
+        for (;;) {
+            if (!done) {
+                if (k < kend) {
+                    const float4 pj = sp[k];
+                    if (r2_cells(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z) < 4.0f) s_list[(n++) * T + threadIdx.x] = (unsigned short)k;
+                    ++k;
+                } else if (++jy > ly + STENCIL && (jy = ly - STENCIL, ++jz > zhi)) {
+                    done = true;
+                } else {
+                    const int la = (jz * G::RY + jy) * G::RX + lx - STENCIL;
+                    k = s_off[la];
+                    kend = s_off[la + 5];
+                }
+            }
+            if (__any_sync(0xffffffffu, n == DLIST)) ASPH_DRAIN();
+            if (__all_sync(0xffffffffu, done)) break;
+        }
+        ASPH_DRAIN();
+#undef ASPH_DRAIN
+        if (active) {
+            if (fast) A.nbr_cnt[i] = L.n <= NBR_CAP ? L.n : -1;
+            else density_target_global(P, A, i, pi, s, rr);
+            density_eos_epilogue(P, A.out, i, pi, s, rr, dt);
+        }
+    }
+}
+
+// ===========================================================================
+// M: momentum + integrate + rain + CFL (list-driven)
+// ===========================================================================
+struct MArgs {
+    const float4* pos;     // x, y, z, -
+    const float4* vel;     // velocities after the first half kick
+    const float2* rp;      // rho, p'
+    const int2* range;
+    const int* nbr;
+    const int* nbr_cnt;
+    int use_lists;         // lists were produced on the current positions
+    MOut out;
+    const float* rain_in;
+    const float* rain_delta;
+    float* rain_out;
+    float* precip;
+    DevCtl* ctl;
+    int part_blocks;       // blocks of particle work; the rest advect rain
+};
+
+__global__ __launch_bounds__(M_TPB) void k_momentum(const __grid_constant__ Phys P, const __grid_constant__ MArgs A,
+                                                    int mode) {
+    __shared__ float s_max[3][M_TPB / 32];
+    __shared__ bool s_last;
+    DevCtl* ctl = A.ctl;
+    const bool aborted = ctl->aborted != 0;
+    const float dt = ctl->dt;
+    const bool rain_block = (int)blockIdx.x >= A.part_blocks;
+    float3 m = make_float3(0.f, 0.f, 0.f);
+    if (rain_block) {
+        const int cid = (blockIdx.x - A.part_blocks) * blockDim.x + threadIdx.x;
+        if (cid < P.ncell && !aborted) rain_cell(P, cid, dt, A.rain_in, A.rain_delta, A.rain_out, A.precip);
+    } else {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < P.N) {
+            if (aborted) {
+                if (mode & M_INTEGRATE) A.out.vel_out[i] = A.vel[i];
+            } else {
+                const float4 p = A.pos[i], v = A.vel[i];
+                const float2 r = A.rp[i];
+                MTarget T;
+                T.x = p.x; T.y = p.y; T.z = p.z;
+                T.u = v.x; T.v = v.y; T.w = v.z;
+                T.rhoi = fmaxf(r.x, 1e-3f);
+                T.irhoi = __frcp_rn(T.rhoi);
+                T.pri = r.y;
+                MSum s{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                const int cnt = A.use_lists ? A.nbr_cnt[i] : -1;
+                if (cnt >= 0) {
+                    for (int q = 0; q < cnt; ++q) {
+                        const int j = A.nbr[(size_t)q * P.N + i];
+                        const float4 pj = A.pos[j];
+                        const float2 rj = A.rp[j];
+                        const float4 vj = A.vel[j];
+                        msum_add(P, s, T, make_float4(pj.x, pj.y, pj.z, rj.y), make_float4(vj.x, vj.y, vj.z, rj.x));
+                    }
+                } else {
+                    for_window_global(P, A.range, T.x, T.y, T.z, [&](int j) {
+                        const float4 pj = A.pos[j];
+                        const float r2t = r2_cells(P, T.x, T.y, T.z, pj.x, pj.y, pj.z);
+                        if (r2t >= 4.0f || r2t < 1e-12f) return;   // also excludes j == i
+                        const float2 rj = A.rp[j];
+                        const float4 vj = A.vel[j];
+                        msum_add(P, s, T, make_float4(pj.x, pj.y, pj.z, rj.y), make_float4(vj.x, vj.y, vj.z, rj.x));
+                    });
+                }
+                m = momentum_epilogue(P, A.out, i, T, s, (mode & M_INTEGRATE) != 0, dt);
+            }
+        }
+        if (mode & M_INTEGRATE) {
+            float mx = warp_max(m.x), my = warp_max(m.y), mz = warp_max(m.z);
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            if (lane == 0) { s_max[0][warp] = mx; s_max[1][warp] = my; s_max[2][warp] = mz; }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                float a = 0.f, b = 0.f, c = 0.f;
+                for (int w = 0; w < M_TPB / 32; ++w) {
+                    a = fmaxf(a, s_max[0][w]); b = fmaxf(b, s_max[1][w]); c = fmaxf(c, s_max[2][w]);
+                }
+                atomicMax(&ctl->gmax[0], __float_as_uint(a));
+                atomicMax(&ctl->gmax[1], __float_as_uint(b));
+                atomicMax(&ctl->gmax[2], __float_as_uint(c));
+            }
+        }
+    }
+    if (mode & M_CFL) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            const unsigned t = atomicAdd(&ctl->done, 1u);
+            s_last = (t == gridDim.x - 1);
+        }
+        __syncthreads();
+        if (s_last && threadIdx.x == 0) {
+            __threadfence();
+            ctl->done = 0u;
+            if (!ctl->aborted) cfl_control(P, ctl);
+        }
+    }
+}
+
+// ===========================================================================
+// launch
+// ===========================================================================
+namespace {
+
+struct Shape {
+    int bx, by, bz;
+};
+constexpr Shape SHAPES[] = {{8, 8, 8}, {8, 8, 4}, {8, 4, 4}, {4, 4, 4}};
+constexpr int MAX_STAGE = 4096;      // staged particles per brick at most
+constexpr double STAGE_MARGIN = 1.35;
+
+int region_cells(const Shape& s) { return (s.bx + 2 * HALO) * (s.by + 2 * HALO) * (s.bz + 2 * HALO); }
+
+// Largest brick whose region fits the grid without wrapping onto itself
+// and whose expected staged count (with a margin) fits the cap.
+int pick_shape(const Phys& P) {
+    const double ppc = (double)P.N / (double)P.ncell;
+    for (int k = 0; k < 4; ++k) {
+        const Shape& s = SHAPES[k];
+        if (P.nx < s.bx + 2 * HALO || P.ny < s.by + 2 * HALO) continue;
+        if (region_cells(s) * ppc * STAGE_MARGIN <= MAX_STAGE) return k;
+    }
+    return -1;
+}
+
+struct Launch {
+    PairCfg C;
+    int threads;
+    size_t smem;
+};
+
+Launch plan(const Phys& P, const Shape& s) {
+    Launch L;
+    L.C.nbx = (P.nx + s.bx - 1) / s.bx;
+    L.C.nby = (P.ny + s.by - 1) / s.by;
+    L.C.nbz = (P.nz + s.bz - 1) / s.bz;
+    L.C.nbricks = L.C.nbx * L.C.nby * L.C.nbz;
+    const double ppc = (double)P.N / (double)P.ncell;
+    const int R = region_cells(s);
+    int cap = (int)(R * ppc * STAGE_MARGIN) + 64;
+    cap = (cap + 63) & ~63;
+    L.C.cap = cap > MAX_STAGE ? MAX_STAGE : cap;
+    // about one thread per expected target (the lattice keeps brick counts
+    // close to the mean), in whole warps, 64..512
+    int t = (int)(s.bx * s.by * s.bz * ppc * 1.04 + 31) / 32 * 32;
+    L.threads = t < 64 ? 64 : (t > 512 ? 512 : t);
+    const size_t queue = (size_t)DLIST * L.threads * 2, start = (size_t)4 * R;
+    L.smem = (size_t)L.C.cap * 16 + (size_t)L.C.cap * 4 + (size_t)4 * (R + 1) + (queue > start ? queue : start);
+    return L;
+}
+
+template <int BX, int BY, int BZ>
+void launch_d(const Phys& P, const DArgs& A, cudaStream_t s) {
+    const Launch L = plan(P, Shape{BX, BY, BZ});
+    cudaFuncSetAttribute(k_density_brick<BX, BY, BZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+    k_density_brick<BX, BY, BZ><<<L.C.nbricks, L.threads, L.smem, s>>>(P, A, L.C);
+}
+
+inline int blocks_for(int n, int tpb) { return n <= 0 ? 1 : (n + tpb - 1) / tpb; }
+
+}  // namespace
+
+int pair_shape(const Phys& P) { return pick_shape(P); }
+
+void launch_density(const Phys& P, const Bufs& B, cudaStream_t s) {
+    DArgs A;
+    A.pos = B.pos[B.pc];
+    A.range = B.range;
+    A.skeys = B.skeys;
+    A.out.thq = B.thq[B.qc];
+    A.out.rp = B.rp;
+    const bool reads = P.accretion || P.rain_evap;
+    A.out.rain_cur = B.rain[B.rc];
+    A.out.rain_dep = reads ? B.rain_delta : B.rain[B.rc];
+    A.nbr = B.nbr;
+    A.nbr_cnt = B.nbr_cnt;
+    A.ctl = B.ctl;
+    switch (B.force_global ? -1 : pick_shape(P)) {
+        case 0: launch_d<8, 8, 8>(P, A, s); break;
+        case 1: launch_d<8, 8, 4>(P, A, s); break;
+        case 2: launch_d<8, 4, 4>(P, A, s); break;
+        case 3: launch_d<4, 4, 4>(P, A, s); break;
+        default: k_density_global<<<blocks_for(P.N, 256), 256, 0, s>>>(P, A); break;
+    }
+}
+
+void launch_momentum(const Phys& P, const Bufs& B, int mode, int use_lists, cudaStream_t s) {
+    MArgs A;
+    A.pos = B.pos[B.pc];
+    A.vel = B.vel[B.vc];
+    A.rp = B.rp;
+    A.range = B.range;
+    A.nbr = B.nbr;
+    A.nbr_cnt = B.nbr_cnt;
+    A.use_lists = use_lists;
+    A.out.thq = B.thq[B.qc];
+    A.out.acc = B.acc;
+    A.out.dthdt = B.dthdt;
+    A.out.vel_out = B.vel[1 - B.vc];
+    A.rain_in = B.rain[B.rc];
+    A.rain_delta = (P.accretion || P.rain_evap) ? B.rain_delta : nullptr;
+    A.rain_out = B.rain[1 - B.rc];
+    A.precip = B.precip;
+    A.ctl = B.ctl;
+    A.part_blocks = blocks_for(P.N, M_TPB);
+    const int rain_blocks = (mode & M_RAIN) ? blocks_for(P.ncell, M_TPB) : 0;
+    k_momentum<<<A.part_blocks + rain_blocks, M_TPB, 0, s>>>(P, A, mode);
+}
+
+}  // namespace asph

@@ -56,6 +56,11 @@ struct Phys {
     float cfl, dt_cap, dt_floor, dt_static;
     int   max_trip, strict_cfl, adaptive_dt, sort_every, permute_acc;
     int   key_bits;    // 3*ceil_log2(max n) (asph_h100.cu:866-868)
+    // reference-sounding tables, one node per metre of height (device)
+    const float4* snd_rho;    // rho_ref
+    const float4* snd_p;      // pres_ref
+    const float4* snd_thvr;   // theta_ref * (1 + 0.608 qv_ref)
+    int   snd_n;              // nodes
 };
 
 // ---- SPH kernel (asph_h100.cu:125-134) -----------------------------------

@@ -39,6 +39,12 @@ def _case(name):
     if name == "single":
         p = small_config(lat=(1, 1, 1))
         return p, random_state(p, 6, "uniform")
+    if name == "ref_fast":   # drift of more than one cell since the sort
+        p = reference_geometry(16, 16, 12)
+        return p, random_state(p, 10, "jitter", speed=500.0)
+    if name == "cfg_wide":   # the largest brick shape on a wider grid
+        p = small_config(lat=(24, 24, 24), grid=(30, 30, 60), box=(6000.0, 6000.0, 3000.0))
+        return p, random_state(p, 12, "jitter")
     raise ValueError(name)
 
 
@@ -103,7 +109,7 @@ def test_sort_full_size_cfg1_bit_exact():
     _check_sort(p, s)
 
 
-def _stages(p, s, simt=1500.0):
+def _stages(p, s, simt=1500.0, global_path=False, tol=None):
     """Run sort -> kick/drift/flux -> density/EOS -> momentum -> rain -> CFL
     on the GPU, checking each stage against the oracle fed the GPU's
     previous-stage output."""
@@ -111,6 +117,9 @@ def _stages(p, s, simt=1500.0):
     C = p.nx * p.ny * p.nz
     rain0 = np.where(rng.uniform(size=C) < .3, rng.uniform(0, 3e4, C), 0.0).astype(np.float32)
     sim = _ctx(p, s, rain0)
+    sim.set_pair_path(global_path)
+    if not global_path:
+        assert sim.pair_shape() >= 0, "brick path not applicable to this grid"
     sim.sort_build()
     ctl = sim.control()
     dt = float(np.float32(ctl["dt_cap"]))
@@ -140,7 +149,8 @@ def _stages(p, s, simt=1500.0):
     mo = sim.get_state()
     omo = oracle.momentum(p, as64(de), srt["cell_range"], dt, integrate=True)
     for k in ("ax", "ay", "az", "dthdt", "th", "u", "v", "w"):
-        assert normwise(mo[k], omo[k]) < TOL, ("momentum", k, normwise(mo[k], omo[k]))
+        t = (tol or {}).get(k, TOL)
+        assert normwise(mo[k], omo[k]) < t, ("momentum", k, normwise(mo[k], omo[k]))
     # rain sedimentation (deposits of this step included)
     sim.rain()
     rain, precip = sim.get_rain()
@@ -161,9 +171,15 @@ def _stages(p, s, simt=1500.0):
     sim.close()
 
 
-@pytest.mark.parametrize("name", ["ref_jitter", "ref_cluster", "cfg_jitter", "cfg_uniform"])
-def test_stages_match_oracle(name):
-    _stages(*_case(name))
+@pytest.mark.parametrize("name", ["ref_jitter", "ref_cluster", "ref_fast", "cfg_jitter", "cfg_uniform", "cfg_wide"])
+@pytest.mark.parametrize("path", ["brick", "global"])
+def test_stages_match_oracle(name, path):
+    # ref_fast moves particles by more than a cell (250-500 m/s, far outside
+    # the CFL envelope) to exercise the staged-region fallback; there the
+    # viscous heating -v.a_visc/(c_p Pi) is a cancellation of O(100) K/s
+    # terms clamped at 1 K/s, resolved by FP32 to ~1e-5 of the cap.
+    tol = {"dthdt": 1e-4} if name == "ref_fast" else None
+    _stages(*_case(name), global_path=(path == "global"), tol=tol)
 
 
 # ---------------------------------------------------------------------------
@@ -197,31 +213,44 @@ def test_stages_match_reference_kernels(case):
         assert normwise(kd[k], g["out_kd_vel"][:, c]) < 1e-6
     for k, c in (("th", 0), ("qv", 1)):
         assert normwise(kd[k], g["out_flux_thq"][:, c]) < 1e-6
-    # density + EOS from the reference's post-drift state
+    # density + EOS from the reference's post-drift state.  Gate: the GPU is
+    # within 1e-5 of the FP64 oracle on the same inputs, and no further from
+    # the reference's own FP32 output than the oracle is (+1e-5).
     pos, vel, fth = g["out_kd_pos"], g["out_kd_vel"], g["out_flux_thq"]
     sim.set_state(dict(x=pos[:, 0], y=pos[:, 1], z=pos[:, 2], u=vel[:, 0], v=vel[:, 1], w=vel[:, 2],
                        th=fth[:, 0], qv=fth[:, 1], qc=fth[:, 2], rho=g["out_g_rho"]))
     sim.set_rain(g["in_rain"])
     sim.density_eos()
     de = sim.get_state()
-    assert normwise(de["rho"], g["out_d_rho"]) < TOL
-    assert normwise(de["prs"], g["out_e_prs"]) < TOL
+    sd = {"x": pos[:, 0], "y": pos[:, 1], "z": pos[:, 2], "th": fth[:, 0], "qv": fth[:, 1], "qc": fth[:, 2]}
+    ode = oracle.density_eos(p, as64(sd), g["out_g_rho"], g["out_cell_range"], dt)
+
+    def gate(gpu, orc, ref, name):
+        e_go, e_or, e_gr = normwise(gpu, orc), normwise(orc, ref), normwise(gpu, ref)
+        assert e_go < TOL, (name, "vs oracle", e_go)
+        assert e_gr <= e_or + TOL, (name, "vs reference", e_gr, "oracle vs reference", e_or)
+
+    gate(de["rho"], ode["rho"], g["out_d_rho"], "rho")
+    gate(de["prs"], ode["prs"], g["out_e_prs"], "prs")
     for k, c in (("th", 0), ("qv", 1), ("qc", 2)):
-        assert normwise(de[k], g["out_e_thq"][:, c]) < TOL, k
+        gate(de[k], ode[k], g["out_e_thq"][:, c], k)
     rain, _ = sim.get_rain()
-    assert normwise(rain, g["out_e_rain"]) < TOL
+    gate(rain, g["in_rain"] + ode["rain_dep"], g["out_e_rain"], "rain")
     # momentum + integrate from the reference's post-EOS state
     eth = g["out_e_thq"]
     sim.set_state(dict(x=pos[:, 0], y=pos[:, 1], z=pos[:, 2], u=vel[:, 0], v=vel[:, 1], w=vel[:, 2],
                        th=eth[:, 0], qv=eth[:, 1], qc=eth[:, 2], rho=g["out_d_rho"], prs=g["out_e_prs"]))
     sim.momentum(True)
     mo = sim.get_state()
+    sm = {"x": pos[:, 0], "y": pos[:, 1], "z": pos[:, 2], "u": vel[:, 0], "v": vel[:, 1], "w": vel[:, 2],
+          "th": eth[:, 0], "qv": eth[:, 1], "qc": eth[:, 2], "rho": g["out_d_rho"], "prs": g["out_e_prs"]}
+    omo = oracle.momentum(p, as64(sm), g["out_cell_range"], dt, integrate=True)
     for k, c in (("ax", 0), ("ay", 1), ("az", 2)):
-        assert normwise(mo[k], g["out_m_acc"][:, c]) < TOL, k
-    assert normwise(mo["dthdt"], g["out_m_dthdt"]) < TOL
-    assert normwise(mo["th"], g["out_i_thq"][:, 0]) < TOL
+        gate(mo[k], omo[k], g["out_m_acc"][:, c], k)
+    gate(mo["dthdt"], omo["dthdt"], g["out_m_dthdt"], "dthdt")
+    gate(mo["th"], omo["th"], g["out_i_thq"][:, 0], "th")
     for k, c in (("u", 0), ("v", 1), ("w", 2)):
-        assert normwise(mo[k], g["out_i_vel"][:, c]) < TOL, k
+        gate(mo[k], omo[k], g["out_i_vel"][:, c], k)
     sim.set_rain(g["out_e_rain"], np.zeros(p.nx * p.ny, np.float32))
     sim.rain()
     rain, precip = sim.get_rain()
@@ -244,7 +273,21 @@ def test_init_matches_reference_kernels():
     assert normwise(st["th"], g["thq"][:, 0]) < TOL
     assert normwise(st["qv"], g["thq"][:, 1]) < TOL
     assert normwise(st["rho"], g["rho"]) < TOL
-    assert normwise(st["az"], g["acc"][:, 2]) < TOL
+    # the initial acceleration is a near-equilibrium residual (hydrostatic
+    # lattice): compare the GPU with the FP64 oracle on the GPU's own
+    # initial state, and with the reference within the reference's own
+    # FP32 error against that oracle
+    dt = float(np.float32(sim.control()["dt"]))
+    cr = gs["cell_range"]
+    s2 = {k: st[k].astype(np.float64) for k in st}
+    ode = oracle.density_eos(p, s2, st["rho"], cr, dt)   # st rho is already the density pass output
+    omo = oracle.momentum(p, dict(s2, rho=st["rho"].astype(np.float64), prs=st["prs"].astype(np.float64)), cr, dt,
+                          integrate=False)
+    for k, c in (("ax", 0), ("ay", 1), ("az", 2)):
+        e_go = normwise(st[k], omo[k])
+        e_or = normwise(omo[k], g["acc"][:, c])
+        assert e_go < TOL, (k, e_go)
+        assert normwise(st[k], g["acc"][:, c]) <= e_or + TOL, k
     sim.close()
 
 
@@ -268,7 +311,8 @@ def test_graph_step_equals_granular_blocks():
 
 
 def test_steps_deterministic_and_conserve_water():
-    p = small_config(lat=(16, 16, 16), accretion=0, rain_evap=0, surface_flux=0, sort_every=1)
+    # supersaturated start so that condensation and autoconversion run
+    p = small_config(lat=(16, 16, 16), accretion=0, rain_evap=0, surface_flux=0, sort_every=1, rh=1.2, rh_bl=1.2)
     sims = []
     for _ in range(2):
         sim = Asph(p)
@@ -293,7 +337,7 @@ def test_steps_deterministic_and_conserve_water():
 
 def test_cfl_trip_clamps_and_strict_aborts():
     p = reference_geometry(16, 16, 8)
-    s = random_state(p, 8, "jitter", speed=300.0)
+    s = random_state(p, 8, "jitter", speed=3000.0)
     sim = _ctx(p, s)
     sim.step(1)
     c = sim.control()
@@ -307,7 +351,7 @@ def test_cfl_trip_clamps_and_strict_aborts():
         sim2.step(3)
     assert e.value.status == abi.ASPH_ERR_CFL_ABORT
     c2 = sim2.control()
-    assert c2["aborted"] == 1 and c2["step"] == 0
+    assert c2["aborted"] == 1 and c2["step"] == 1
     frozen = sim2.get_state()
     with pytest.raises(AsphError):
         sim2.step(2)

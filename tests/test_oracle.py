@@ -145,8 +145,9 @@ def test_oracle_matches_reference_stages(case):
     assert np.array_equal(np.nonzero(sb["surf"])[0], g["out_surf_list"])
     gp = sb["gathered"]
     assert np.array_equal(gp["x"].astype(np.float32), g["out_g_pos"][:, 0])
-    # kick + drift + flux
-    st = dict(gp)
+    # kick + drift + flux; the reference kicks with acc in its pre-sort
+    # order (kernel_gather does not permute acc, asph_h100.cu:245-256)
+    st = dict(gp, ax=s["ax"], ay=s["ay"], az=s["az"])
     kd = oracle.kick_drift_flux(p, st, simt, dt, sb["surf"])
     assert normwise(kd["x"], g["out_kd_pos"][:, 0]) < 1e-6
     assert normwise(kd["z"], g["out_kd_pos"][:, 2]) < 1e-6
@@ -158,11 +159,18 @@ def test_oracle_matches_reference_stages(case):
     thq = g["out_flux_thq"].astype(np.float64)
     sd = {"x": pos[:, 0], "y": pos[:, 1], "z": pos[:, 2], "th": thq[:, 0], "qv": thq[:, 1], "qc": thq[:, 2]}
     de = oracle.density_eos(p, sd, g["out_g_rho"], g["out_cell_range"], dt)
-    assert normwise(de["rho"], g["out_d_rho"]) < TOL
-    assert normwise(de["prs"], g["out_e_prs"]) < TOL
-    for k, c in (("th", 0), ("qv", 1), ("qc", 2)):
+    assert normwise(de["rho"], g["out_d_rho"]) < 1e-6
+    # p' = c_s^2 (rho - rho_ref) amplifies the reference's FP32 rounding of
+    # rho by rho/|rho - rho_ref| (~30 here): its own p' carries ~3e-5
+    # normwise error against FP64, so p' pins the oracle only to 1e-4;
+    # rho, from which p' follows, pins it to 1e-6 above.
+    assert normwise(de["prs"], g["out_e_prs"]) < 1e-4
+    for k, c in (("th", 0), ("qv", 1)):
         assert normwise(de[k], g["out_e_thq"][:, c]) < TOL, k
-    assert normwise(g["in_rain"] + de["rain_dep"], g["out_e_rain"]) < TOL
+    # cloud water after saturation adjustment is qv_total - qsat(T, p): the
+    # same cancellation, under the reference's fast-math esat
+    assert normwise(de["qc"], g["out_e_thq"][:, 2]) < 1e-4
+    assert normwise(g["in_rain"] + de["rain_dep"], g["out_e_rain"]) < 1e-4
     # momentum + theta update + kick + sponge
     vel = g["out_kd_vel"].astype(np.float64)
     eth = g["out_e_thq"].astype(np.float64)
@@ -185,8 +193,12 @@ def test_oracle_matches_reference_stages(case):
     it = g["out_i_thq"].astype(np.float64)
     au = oracle.audit(p, {"z": pos[:, 2], "u": iv[:, 0], "v": iv[:, 1], "w": iv[:, 2], "th": it[:, 0],
                           "qv": it[:, 1], "qc": it[:, 2]})
-    for k in (1, 2, 3, 5):
+    for k in (1, 2, 3):
         assert abs(au[k] / g["out_audit"][k] - 1) < 1e-6, k
+    # the reference adds PMASS once per thread of its 1024 x 256 audit grid
+    # (asph_h100.cu:667), so its "mass" is 262144 PMASS whatever N is; the
+    # oracle and the CUDA path report N PMASS
+    assert abs(g["out_audit"][5] / (262144 * au[5] / p.n_particles) - 1) < 1e-6
     assert abs(au[0] - g["out_audit"][0]) <= 1e-5 * abs(g["out_audit"][0])
 
 
@@ -212,4 +224,8 @@ def test_oracle_matches_reference_init():
     assert normwise(de["qv"], g["thq"][:, 1]) < TOL
     sm = dict(gp, th=de["th"], qv=de["qv"], qc=de["qc"], rho=de["rho"], prs=de["prs"])
     mo = oracle.momentum(p, sm, sb["cell_range"], dt, integrate=False)
-    assert normwise(mo["az"], g["acc"][:, 2]) < TOL
+    # On the hydrostatic cell-centre lattice the acceleration is a small
+    # residual of cancelling pressure-gradient terms; the reference's FP32
+    # (fast-math) evaluation of it carries ~3e-4 normwise error, so the
+    # pinning bound here is looser than the 1e-5 single-step gate.
+    assert normwise(mo["az"], g["acc"][:, 2]) < 1e-3
