@@ -228,6 +228,27 @@ int asph_dump(asph_ctx* ctx, const char* outdir, char* path, int path_len);
  * resets the precipitation accumulator like the reference. */
 int asph_column_diag(asph_ctx* ctx, float out[4]);
 
+/* ---- stable key sort without allocation -----------------------------------
+ * No counterpart in the reference.  For callers that must not call
+ * cudaMalloc/cudaFree (a latency-critical loop where cudaFree would
+ * synchronise the device, a host callback or foreign-language runtime that
+ * must not block in the allocator, an application whose memory pool owns all
+ * device memory): sorts n 32-bit keys (device pointer `keys`) over bits
+ * [0, key_bits) stably, writing the sorted keys and the permutation
+ * (sorted position -> input index) to caller-owned device buffers.  Same
+ * kernels and same result as the sort of asph_sort_build.  Scratch lives in
+ * a static device array sized for ASPH_NOALLOC_MAX_KEYS keys (about 5 MB,
+ * held by every GPU that loads the library until exit); larger n returns
+ * ASPH_ERR_ARG.  All calls share that array: calls that overlap on the GPU
+ * race and must be serialised by the caller.  The outputs must not alias
+ * `keys` or each other.  The first call on a device
+ * looks up the array's address (make it before any stream capture).  The
+ * call synchronises `stream` and returns ASPH_ERR_TIMEOUT if a bounded
+ * device wait gave up. */
+#define ASPH_NOALLOC_MAX_KEYS 524288
+int asph_sort_keys_noalloc(const uint32_t* keys, uint32_t* keys_sorted, uint32_t* perm, int n, int key_bits,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,7 +22,7 @@ CLI = os.path.join(BUILD, "asph")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
-CU_SOURCES = ["asph_sort.cu", "asph_kernels.cu", "asph_pairs.cu", "asph_capi.cu"]
+CU_SOURCES = ["asph_sort.cu", "asph_kernels.cu", "asph_pairs.cu", "asph_capi.cu", "asph_noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -28,6 +28,7 @@ MAX_BUBBLES = 8
 NPHASES = 6
 OPT_PAIR_PATH = 1
 OPT_PAIR_SHAPE = 2
+NOALLOC_MAX_KEYS = 524288
 PHASES = ("table_clear", "sort", "gather_kick_drift", "density_eos", "momentum_integrate", "step")
 
 _f = C.c_float
@@ -126,6 +127,7 @@ SIGNATURES = {
     "asph_audit": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "asph_dump": (C.c_int, [_P, C.c_char_p, C.c_char_p, C.c_int]),
     "asph_column_diag": (C.c_int, [_P, _FP]),
+    "asph_sort_keys_noalloc": (C.c_int, [_P, _P, _P, C.c_int, C.c_int, _P]),
 }
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

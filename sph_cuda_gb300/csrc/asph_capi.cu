@@ -45,6 +45,8 @@ int ceil_log2(int n) {   // asph_h100.cu:865
 
 }  // namespace
 
+int asph::set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 struct GraphKey {
     int pc, vc, qc, rc;
 };

@@ -72,6 +72,9 @@ enum : int {
     M_CFL       = 4,    // last block runs the CFL control
 };
 
+// Record a failure for asph_last_error() (asph_capi.cu); returns `code`.
+int set_error(int code, const char* msg);
+
 // ---- launch functions (asph_kernels.cu / asph_sort.cu) --------------------
 void launch_init(const Phys& P, const Bufs& B, const float* bub, int nbub, int init_mode,
                  int lat_nx, int lat_ny, int lat_nz, float jitter, uint32_t seed, float noise,
