@@ -1,7 +1,6 @@
 """Benchmark: particle-steps/s of the full SPH warm-rain step.
 
-Workload: the 2,097,152-particle moist-bubble configuration (cfg1:
-128^3 jittered lattice in a 20 x 20 x 8 km box, cells 150.4 x 150.4 x 40 m,
+Workload: the 2,097,152-particle moist-bubble configuration (128^3 jittered lattice in a 20 x 20 x 8 km box, cells 150.4 x 150.4 x 40 m,
 three seeded warm bubbles, warm rain with accretion and evaporation, Morton
 re-sort every step).  Synthetic, seeded initial state; no dataset.
 
@@ -111,11 +110,11 @@ def dist_setup():
 
 
 def cpu_sample_params():
-    """cfg1 physics on a quarter-width box: 32 x 32 x 128 lattice (131,072
+    """The moist-bubble physics on a quarter-width box: 32 x 32 x 128 lattice (131,072
     particles), 33 x 33 x 200 cells of the same 150.4 x 150.4 x 40 m size, so
     the per-particle neighbour work equals the full workload's."""
     import sph_cuda_gb300 as sph
-    p = sph.preset("cfg1")
+    p = sph.preset("bubble2m")
     p.nx = p.ny = 33
     p.lat_nx = p.lat_ny = 32
     p.n_particles = 32 * 32 * 128
@@ -154,10 +153,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": "cfg1 moist bubble (sample: 131,072-particle quarter box)",
+        "data": "synthetic", "config": {"workload": "moist bubble (sample: 131,072-particle quarter box)",
                                        "particles": p.n_particles, "cells": p.nx * p.ny * p.nz},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "%d full FP64 steps of the 131,072-particle quarter-box cfg1 sample" % args.steps},
+                         "sample": "%d full FP64 steps of the 131,072-particle quarter-box moist-bubble sample" % args.steps},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -175,7 +174,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     stream = torch.cuda.Stream()
-    p = sph.preset("cfg1")
+    p = sph.preset("bubble2m")
     N, C = p.n_particles, p.nx * p.ny * p.nz
     sim = sph.Asph(p, stream=stream.cuda_stream)
     sim.init()
@@ -221,7 +220,7 @@ def run_ours(args):
     hbm, src = peaks()
     achieved = algo[dom] / (ph_ms[dom] / 1e3) / 1e9
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic_cfg1.json.txt")
+    tfile = os.path.join(ROOT, "profiles", "traffic_bubble2m.json.txt")
     if os.path.exists(tfile):
         try:
             traffic = json.load(open(tfile)).get(dom)
@@ -253,7 +252,7 @@ def run_ours(args):
         st = oracle_initial_state(ps)
         tc, cores, _ = time_oracle(ps, st, args.cpu_steps)
         cpu = {"value": ps.n_particles * args.cpu_steps / tc, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": "%d full FP64 steps of the 131,072-particle quarter-box cfg1 sample (%.1f s)"
+               "sample": "%d full FP64 steps of the 131,072-particle quarter-box moist-bubble sample (%.1f s)"
                          % (args.cpu_steps, tc)}
 
     ctl = sim.control()
@@ -262,7 +261,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "cfg1 moist bubble, 2,097,152 particles, 133x133x200 cells, sort every step",
+            "config": {"workload": "moist bubble, 2,097,152 particles, 133x133x200 cells, sort every step",
                        "particles": N, "cells": C, "dt_s": ctl["dt"],
                        "l2": "working set %.0f MB > 129 MB L2 (no flush needed)" % ((N * 164 + C * 20) / 1e6),
                        "parallelism": "replicas x%d" % ws},

@@ -45,13 +45,16 @@ extern "C" {
 #define ASPH_ERR_NOMEM      6   /* device or host allocation failed */
 #define ASPH_ERR_IO         7   /* dump file could not be written */
 #define ASPH_ERR_STATE      8   /* call out of order (e.g. step before init) */
+#define ASPH_ERR_NONFINITE  9   /* a particle position or velocity became NaN/Inf; the run was stopped */
+#define ASPH_ERR_DENSE     10   /* a search window held more than ASPH_MAX_CANDIDATES particles; the run was stopped */
+#define ASPH_MAX_CANDIDATES 65536
 
 /* ---- parameter presets ------------------------------------------------- */
 #define ASPH_PRESET_REFERENCE 0 /* the reference's constexpr physics, 1 particle per cell (asph_h100.cu:48-120) */
-#define ASPH_PRESET_CFG0      1 /* 65,536 particles, 10x10x5 km, h 200/50 m, one bubble */
-#define ASPH_PRESET_CFG1      2 /* 2,097,152 particles, 20x20x8 km, h 150/40 m, three bubbles, sort every step */
-#define ASPH_PRESET_CFG2      3 /* 16,777,216 particles, 40x40x10 km, h 160/20 m, 95% RH below 1 km */
-#define ASPH_PRESET_CFG3      4 /* 262,144 particles in the CFG0 box (adjoint workload) */
+#define ASPH_PRESET_SMALL_65K      1 /* 65,536 particles, 10x10x5 km, h 200/50 m, one bubble */
+#define ASPH_PRESET_BUBBLE_2M      2 /* 2,097,152 particles, 20x20x8 km, h 150/40 m, three bubbles, sort every step */
+#define ASPH_PRESET_LARGE_16M      3 /* 16,777,216 particles, 40x40x10 km, h 160/20 m, 95% RH below 1 km */
+#define ASPH_PRESET_ADJOINT_262K      4 /* 262,144 particles in the SMALL_65K box (adjoint workload) */
 
 #define ASPH_INIT_REFERENCE 0   /* one particle at each cell centre + hash noise (asph_h100.cu:210-227) */
 #define ASPH_INIT_LATTICE   1   /* jittered lattice + Gaussian bubbles + Gaussian noise */
@@ -216,6 +219,13 @@ int asph_step_profiled(asph_ctx* ctx, int nsteps, float* phase_ms);
 #define ASPH_OPT_PAIR_SHAPE 2
 int asph_set_option(asph_ctx* ctx, int option, int value);
 int asph_get_option(asph_ctx* ctx, int option, int* value);
+
+/* Neighbour lists of the last density pass (pairs with 0 < q < 2 accepted
+ * by the reference's window rule, asph_h100.cu:296-327): count[i] per
+ * particle (-1 if it overflowed ASPH_NBR_CAP) and list[q*N + i], q < count[i]
+ * (slot-major, N*ASPH_NBR_CAP entries).  Either pointer may be NULL. */
+#define ASPH_NBR_CAP 64
+int asph_get_neighbours(asph_ctx* ctx, int32_t* count, int32_t* list);
 
 /* ---- diagnostics and output ----------------------------------------------- */
 /* FP64 totals: KE, PE, IE, water, p_z, mass (asph_h100.cu:650-668). */

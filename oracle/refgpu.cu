@@ -1,7 +1,7 @@
 // refgpu.cu — TEST INFRASTRUCTURE ONLY: runs the reference's own kernels.
 //
 // The reference's device code (asph_h100.cu, compiled unmodified into
-// oracle/_ref/asph_ref.cubin by oracle/build_ref.sh) is loaded through the
+// oracle/_ref/asph_ref.cubin by oracle/build_oracle.py) is loaded through the
 // CUDA driver API, and this program replays the blocks of the reference's
 // host step loop (asph_h100.cu:958-1078) around those kernels, with the
 // reference's own library sort, cub::DeviceRadixSort::SortPairs
@@ -15,6 +15,7 @@
 //   refgpu <cubin> init <nx> <ny> <nz> <noise> <outdir>
 //   refgpu <cubin> run <nx> <ny> <nz> <steps> <dt> <sort_every>
 //          sort_every 0 = the reference's displacement-gated cadence
+//   refgpu <cubin> runstate <in.bin> <steps> <dx> <dy> <dz>
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
@@ -359,6 +360,65 @@ static int cmd_run(const Ref& R, int nx, int ny, int nz, int steps, float dt_req
     return 0;
 }
 
+// The reference step loop on a given state (cmd_stages input format), a sort
+// every step, for timing: K steps at the state's dt with the reference's
+// per-step velocity maxima read back to the host (asph_h100.cu:1043-1046).
+// Cell sizes are passed because the cubin may carry other constexprs.
+static int cmd_runstate(const Ref& R, const char* in, int steps, float dx, float dy, float dz) {
+    FILE* f = fopen(in, "rb");
+    if (!f) { fprintf(stderr, "cannot open %s\n", in); return 1; }
+    int32_t hdr[8];
+    double simt;
+    float dt;
+    if (fread(hdr, 4, 8, f) != 8 || fread(&simt, 8, 1, f) != 1 || fread(&dt, 4, 1, f) != 1) return 1;
+    Dev d;
+    alloc(d, hdr[1], hdr[2], hdr[3], hdr[4]);
+    read_into(f, d.pos, (size_t)d.N); read_into(f, d.vel, (size_t)d.N); read_into(f, d.thq, (size_t)d.N);
+    read_into(f, d.rho, (size_t)d.N); read_into(f, d.acc, (size_t)d.N);
+    read_into(f, d.rainA, (size_t)d.C); read_into(f, d.precip, (size_t)d.nx * d.ny);
+    fclose(f);
+    launch(R.iota, bpb(d.N), TPB, d.valsIn, d.N);
+    const float Lx = d.nx * dx, Ly = d.ny * dy, Lz = d.nz * dz;
+    float hg[3];
+    auto now = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
+    auto one = [&]() {
+        sort_block(R, d);
+        launch(R.kick, bpb(d.N), TPB, d.vel, (const float4*)d.acc, d.N, 0.5f * dt);
+        launch(R.drift, bpb(d.N), TPB, d.pos, d.vel, d.N, dt, Lx, Ly, Lz);
+        float Ts, qs;
+        flux_targets(simt, Ts, qs);
+        launch(R.flux, bpb(d.surfCap), TPB, d.thq, (const float4*)d.pos, (const int*)d.surfList,
+               (const int*)d.surfCount, d.surfCap, dt, Ts, qs);
+        launch(R.density, bpb(d.N), TPB, (const float4*)d.pos, (const float*)d.rho, (const int2*)d.cellRange, d.rho2,
+               d.nx, d.ny, d.nz, d.N);
+        std::swap(d.rho, d.rho2);
+        launch(R.eos, bpb(d.N), TPB, d.thq, (const float4*)d.pos, (const float*)d.rho, d.prs, d.rainA, d.nx, d.ny,
+               d.nz, d.N, dt);
+        launch(R.momentum, bpb(d.N), TPB, (const float4*)d.pos, (const float4*)d.vel, (const float4*)d.thq,
+               (const float*)d.rho, (const float*)d.prs, (const int2*)d.cellRange, d.acc, d.dthdt, d.nx, d.ny, d.nz,
+               d.N);
+        launch(R.theta, bpb(d.N), TPB, d.thq, (const float*)d.dthdt, d.N, dt);
+        launch(R.kick, bpb(d.N), TPB, d.vel, (const float4*)d.acc, d.N, 0.5f * dt);
+        launch(R.sponge, bpb(d.N), TPB, d.pos, d.vel, d.N, dt, Lz);
+        launch(R.rain, bpb(d.C), TPB, (const float*)d.rainA, d.rainB, d.precip, d.nx, d.ny, d.nz, dt);
+        std::swap(d.rainA, d.rainB);
+        simt += dt;
+        CK(cudaMemsetAsync(d.gmax, 0, 12));
+        launch(R.maxvel, 1024, TPB, (const float4*)d.vel, d.N, d.gmax);
+        CK(cudaMemcpy(hg, d.gmax, 12, cudaMemcpyDeviceToHost));
+    };
+    for (int k = 0; k < 3; ++k) one();   // warm-up
+    CK(cudaDeviceSynchronize());
+    const double t0 = now();
+    for (int k = 0; k < steps; ++k) one();
+    CK(cudaDeviceSynchronize());
+    const double wall = now() - t0;
+    printf("{\"impl\": \"reference-gpu\", \"N\": %d, \"cells\": %d, \"steps\": %d, \"wall_s\": %.6f, "
+           "\"particle_steps_per_s\": %.6e, \"ms_per_step\": %.6f, \"wmax\": %.4f}\n",
+           d.N, d.C, steps, wall, (double)d.N * steps / wall, 1e3 * wall / steps, hg[2]);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 3) {
         fprintf(stderr, "usage: refgpu <cubin> stages|init|run ...\n");
@@ -373,6 +433,9 @@ int main(int argc, char** argv) {
     if (cmd == "run" && argc == 9)
         return cmd_run(R, atoi(argv[3]), atoi(argv[4]), atoi(argv[5]), atoi(argv[6]), (float)atof(argv[7]),
                        atoi(argv[8]));
+    if (cmd == "runstate" && argc == 8)
+        return cmd_runstate(R, argv[3], atoi(argv[4]), (float)atof(argv[5]), (float)atof(argv[6]),
+                            (float)atof(argv[7]));
     fprintf(stderr, "bad arguments\n");
     return 1;
 }

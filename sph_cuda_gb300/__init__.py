@@ -4,7 +4,7 @@ Python host mirror of the C ABI in include/asph.h.  Every method is one C
 call into libasph.so; there is no Python or CPU implementation of any step,
 so a missing or unloadable library raises immediately.
 
-    p = sph_cuda_gb300.preset("cfg1")
+    p = sph_cuda_gb300.preset("bubble2m")
     sim = sph_cuda_gb300.Asph(p)
     sim.init()
     sim.step(500)
@@ -24,10 +24,10 @@ __all__ = ["Asph", "AsphError", "AsphParams", "preset", "library", "STATE_FIELDS
 
 PRESETS = {
     "reference": abi.PRESET_REFERENCE,
-    "cfg0": abi.PRESET_CFG0,
-    "cfg1": abi.PRESET_CFG1,
-    "cfg2": abi.PRESET_CFG2,
-    "cfg3": abi.PRESET_CFG3,
+    "small65k": abi.PRESET_SMALL_65K,
+    "bubble2m": abi.PRESET_BUBBLE_2M,
+    "large16m": abi.PRESET_LARGE_16M,
+    "adjoint262k": abi.PRESET_ADJOINT_262K,
 }
 
 
@@ -48,7 +48,7 @@ def _check(st: int) -> None:
                         or lib.asph_status_string(st).decode())
 
 
-def preset(name: str = "cfg1", nx: int = 0, ny: int = 0, nz: int = 0, **overrides) -> AsphParams:
+def preset(name: str = "bubble2m", nx: int = 0, ny: int = 0, nz: int = 0, **overrides) -> AsphParams:
     """Fill AsphParams from a named preset, then apply field overrides."""
     p = AsphParams()
     _check(library().asph_params_preset(C.byref(p), PRESETS[name], nx, ny, nz))
@@ -160,6 +160,14 @@ class Asph:
                                       surf.ctypes.data_as(i32), C.byref(cnt)))
         return {"keys_in": kin, "keys_sorted": ks, "perm": perm, "cell_range": rng.reshape(-1, 2),
                 "surf_list": surf[:cnt.value].copy(), "surf_count": cnt.value}
+
+    def neighbours(self):
+        """(count[N], list[NBR_CAP][N]) of the last density pass."""
+        cnt = np.empty(self.N, np.int32)
+        lst = np.empty((abi.NBR_CAP, self.N), np.int32)
+        i32 = C.POINTER(C.c_int32)
+        _check(self.lib.asph_get_neighbours(self._ctx, cnt.ctypes.data_as(i32), lst.ctypes.data_as(i32)))
+        return cnt, lst
 
     def kick_drift_flux(self) -> None:
         _check(self.lib.asph_kick_drift_flux(self._ctx))

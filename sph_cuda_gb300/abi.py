@@ -13,12 +13,15 @@ ASPH_ERR_ARG = 5
 ASPH_ERR_NOMEM = 6
 ASPH_ERR_IO = 7
 ASPH_ERR_STATE = 8
+ASPH_ERR_NONFINITE = 9
+ASPH_ERR_DENSE = 10
+MAX_CANDIDATES = 65536
 
 PRESET_REFERENCE = 0
-PRESET_CFG0 = 1
-PRESET_CFG1 = 2
-PRESET_CFG2 = 3
-PRESET_CFG3 = 4
+PRESET_SMALL_65K = 1
+PRESET_BUBBLE_2M = 2
+PRESET_LARGE_16M = 3
+PRESET_ADJOINT_262K = 4
 
 INIT_REFERENCE = 0
 INIT_LATTICE = 1
@@ -29,6 +32,7 @@ NPHASES = 6
 OPT_PAIR_PATH = 1
 OPT_PAIR_SHAPE = 2
 NOALLOC_MAX_KEYS = 524288
+NBR_CAP = 64
 PHASES = ("table_clear", "sort", "gather_kick_drift", "density_eos", "momentum_integrate", "step")
 
 _f = C.c_float
@@ -128,6 +132,7 @@ SIGNATURES = {
     "asph_dump": (C.c_int, [_P, C.c_char_p, C.c_char_p, C.c_int]),
     "asph_column_diag": (C.c_int, [_P, _FP]),
     "asph_sort_keys_noalloc": (C.c_int, [_P, _P, _P, C.c_int, C.c_int, _P]),
+    "asph_get_neighbours": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
 }
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

@@ -109,6 +109,8 @@ extern "C" const char* asph_status_string(int s) {
         case ASPH_ERR_NOMEM: return "out of memory";
         case ASPH_ERR_IO: return "I/O error";
         case ASPH_ERR_STATE: return "call out of order";
+        case ASPH_ERR_NONFINITE: return "non-finite particle state, run stopped";
+        case ASPH_ERR_DENSE: return "search window above ASPH_MAX_CANDIDATES, run stopped";
         default: return "unknown status";
     }
 }
@@ -161,10 +163,10 @@ extern "C" int asph_params_preset(AsphParams* p, int preset, int nx, int ny, int
             if (nz > 0) p->nz = nz;
             p->n_particles = p->nx * p->ny * p->nz;
             break;
-        case ASPH_PRESET_CFG0:
-        case ASPH_PRESET_CFG3: {
-            const int n = preset == ASPH_PRESET_CFG0 ? 32 : 64;
-            config_physics(p, 10000.f, 10000.f, 5000.f, 200.f, 50.f, n, n, preset == ASPH_PRESET_CFG0 ? 64 : 64);
+        case ASPH_PRESET_SMALL_65K:
+        case ASPH_PRESET_ADJOINT_262K: {
+            const int n = preset == ASPH_PRESET_SMALL_65K ? 32 : 64;
+            config_physics(p, 10000.f, 10000.f, 5000.f, 200.f, 50.f, n, n, preset == ASPH_PRESET_SMALL_65K ? 64 : 64);
             p->n_bubbles = 1;
             p->bubble_x[0] = 5000.f; p->bubble_y[0] = 5000.f; p->bubble_z[0] = 1000.f;
             p->bubble_r[0] = 1000.f; p->bubble_amp[0] = 2.0f;
@@ -172,7 +174,7 @@ extern "C" int asph_params_preset(AsphParams* p, int preset, int nx, int ny, int
             p->sort_every = 0;
             break;
         }
-        case ASPH_PRESET_CFG1: {
+        case ASPH_PRESET_BUBBLE_2M: {
             config_physics(p, 20000.f, 20000.f, 8000.f, 150.f, 40.f, 128, 128, 128);
             p->n_bubbles = 3;
             for (int b = 0; b < 3; ++b) {
@@ -186,7 +188,7 @@ extern "C" int asph_params_preset(AsphParams* p, int preset, int nx, int ny, int
             p->sort_every = 1;
             break;
         }
-        case ASPH_PRESET_CFG2:
+        case ASPH_PRESET_LARGE_16M:
             config_physics(p, 40000.f, 40000.f, 10000.f, 160.f, 20.f, 256, 256, 256);
             p->rh_bl = 0.95f; p->z_bl = 1000.f;
             p->noise = 0.2f;
@@ -431,7 +433,7 @@ static int sync_status(asph_ctx* c) {
     int words[2];
     CKR(cudaMemcpy(words, &c->B.ctl->aborted, sizeof(int), cudaMemcpyDeviceToHost));
     CKR(cudaMemcpy(words + 1, &c->B.ctl->error, sizeof(int), cudaMemcpyDeviceToHost));
-    if (words[1]) return fail(words[1], "device error word %d", words[1]);
+    if (words[1]) return fail(words[1], "%s", asph_status_string(words[1]));
     if (words[0]) return fail(ASPH_ERR_CFL_ABORT, "CFL abort: the scheme is outside its stability envelope");
     return ASPH_OK;
 }
@@ -698,6 +700,16 @@ extern "C" int asph_get_sort(asph_ctx* c, uint32_t* keys_in, uint32_t* keys_sort
         if (surf_count) *surf_count = n;
     }
     CKR(cudaStreamSynchronize(s));
+    return ASPH_OK;
+}
+
+extern "C" int asph_get_neighbours(asph_ctx* c, int32_t* count, int32_t* list) {
+    if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
+    if (!c->lists_valid) return fail(ASPH_ERR_STATE, "no neighbour lists for the current positions");
+    const size_t N = (size_t)c->P.N;
+    if (count) CKR(cudaMemcpyAsync(count, c->B.nbr_cnt, N * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (list) CKR(cudaMemcpyAsync(list, c->B.nbr, N * NBR_CAP * 4, cudaMemcpyDeviceToHost, c->stream));
+    CKR(cudaStreamSynchronize(c->stream));
     return ASPH_OK;
 }
 

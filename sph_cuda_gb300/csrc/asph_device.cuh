@@ -33,6 +33,13 @@ __device__ __forceinline__ FF snd_eval(const float4* __restrict__ tab, int nnode
     return r;
 }
 
+// Stop the run from inside a kernel: record the reason (first one wins)
+// and make every later kernel of the step and of later steps do nothing.
+__device__ __forceinline__ void stop_run(DevCtl* ctl, int code) {
+    atomicCAS(&ctl->error, 0, code);
+    atomicExch(&ctl->aborted, 1);
+}
+
 // Surface skin temperature ramp (asph_h100.cu:989-992).
 __device__ __forceinline__ void surface_targets(const Phys& P, double simt, float& Ts, float& qs_sfc) {
     float r = fminf(fmaxf((float)simt / P.ramp, 0.f), 1.f);

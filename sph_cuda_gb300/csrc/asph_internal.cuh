@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "asph_phys.cuh"
+#include "../../include/asph.h"
 
 namespace asph {
 
@@ -13,7 +14,7 @@ constexpr int SORT_ITEMS = 16;
 constexpr int SORT_TILE = SORT_TPB * SORT_ITEMS;   // keys per radix tile
 constexpr int MAX_PASSES = 4;                      // 30-bit keys / 8-bit digits
 constexpr unsigned SPIN_LIMIT = 1u << 24;          // bounded device waits
-constexpr int NBR_CAP = 64;                        // neighbour-list slots per particle
+constexpr int NBR_CAP = ASPH_NBR_CAP;              // neighbour-list slots per particle
 
 // Device-resident step control: the host variables of the reference step
 // loop (asph_h100.cu:931-942, 1040-1078) live here so that a step needs no

@@ -94,7 +94,7 @@ struct GArgs {
 __global__ __launch_bounds__(TPB) void k_gather(const __grid_constant__ Phys P, const __grid_constant__ GArgs A,
                                                 int mode) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const DevCtl* ctl = A.ctl;
+    DevCtl* ctl = A.ctl;
     const bool aborted = ctl->aborted != 0;
     const bool sorted = (mode & G_SORTED) && (((mode & G_FORCE) != 0) || (ctl->do_sort && !aborted));
     const bool integ = (mode & G_INTEGRATE) && !aborted;
@@ -106,72 +106,74 @@ __global__ __launch_bounds__(TPB) void k_gather(const __grid_constant__ Phys P, 
         s_Ts = Ts; s_qs = qs; s_dt = ctl->dt; s_clamp = ctl->clamp_pending;
     }
     __syncthreads();
-    if (i >= P.N) return;
-
-    const int s = sorted ? (int)A.perm[i] : i;
-    float4 p = A.pos_src[s];
-    float4 v = A.vel_src[s];
-    float4 t = A.thq_src[s];
-    const float rho = A.rp[s].x;
-    bool surf;
-    if (sorted) {
-        // keys decode to cells inside the grid; the bounds test only guards
-        // against a sort that gave up (error word set)
-        const uint32_t kc = A.skeys[i];
-        const int c = cid_of_key(P, kc);
-        const bool cin = (unsigned)c < (unsigned)P.ncell;
-        if (i == 0) {
-            if (cin) A.range[c].x = 0;
+    if (i < P.N) {
+        const int s = sorted ? (int)A.perm[i] : i;
+        float4 p = A.pos_src[s];
+        float4 v = A.vel_src[s];
+        float4 t = A.thq_src[s];
+        const float rho = A.rp[s].x;
+        bool surf;
+        if (sorted) {
+            // keys decode to cells inside the grid; the bounds test only guards
+            // against a sort that gave up (error word set)
+            const uint32_t kc = A.skeys[i];
+            const int c = cid_of_key(P, kc);
+            const bool cin = (unsigned)c < (unsigned)P.ncell;
+            if (i == 0) {
+                if (cin) A.range[c].x = 0;
+            } else {
+                const uint32_t kp = A.skeys[i - 1];
+                if (kc != kp) {
+                    const int cp = cid_of_key(P, kp);
+                    if (cin) A.range[c].x = i;
+                    if ((unsigned)cp < (unsigned)P.ncell) A.range[cp].y = i;
+                }
+            }
+            if (i == P.N - 1 && cin) A.range[c].y = P.N;
+            surf = ((int)__fmul_rn(p.z, P.inv_dz)) == 0;
+            A.surf[i] = surf ? 1 : 0;
+            const unsigned m = __ballot_sync(__activemask(), surf);
+            if (surf && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd((int*)&ctl->surf_count, __popc(m));
         } else {
-            const uint32_t kp = A.skeys[i - 1];
-            if (kc != kp) {
-                const int cp = cid_of_key(P, kp);
-                if (cin) A.range[c].x = i;
-                if ((unsigned)cp < (unsigned)P.ncell) A.range[cp].y = i;
+            surf = A.surf[i] != 0;
+        }
+        if (integ) {
+            const float dt = s_dt;
+            if (s_clamp) {
+                const float vmax = 0.5f * P.cs;
+                const float s2 = v.x * v.x + v.y * v.y + v.z * v.z;
+                if (s2 > vmax * vmax) {
+                    const float f = vmax / sqrtf(s2);
+                    v.x *= f; v.y *= f; v.z *= f;
+                }
             }
-        }
-        if (i == P.N - 1 && cin) A.range[c].y = P.N;
-        surf = ((int)__fmul_rn(p.z, P.inv_dz)) == 0;
-        A.surf[i] = surf ? 1 : 0;
-        const unsigned m = __ballot_sync(__activemask(), surf);
-        if (surf && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd((int*)&A.ctl->surf_count, __popc(m));
-    } else {
-        surf = A.surf[i] != 0;
-    }
-
-    if (integ) {
-        const float dt = s_dt;
-        if (s_clamp) {
-            const float vmax = 0.5f * P.cs;
-            const float s2 = v.x * v.x + v.y * v.y + v.z * v.z;
-            if (s2 > vmax * vmax) {
-                const float f = vmax / sqrtf(s2);
-                v.x *= f; v.y *= f; v.z *= f;
+            const float4 a = A.acc[P.permute_acc ? s : i];
+            const float hdt = 0.5f * dt;
+            v.x += a.x * hdt; v.y += a.y * hdt; v.z += a.z * hdt;
+            p.x += v.x * dt; p.y += v.y * dt; p.z += v.z * dt;
+            for (int k = 0; k < 64 && p.x < 0.f; ++k) p.x += P.lx;
+            for (int k = 0; k < 64 && p.x >= P.lx; ++k) p.x -= P.lx;
+            for (int k = 0; k < 64 && p.y < 0.f; ++k) p.y += P.ly;
+            for (int k = 0; k < 64 && p.y >= P.ly; ++k) p.y -= P.ly;
+            if (p.z < 0.f) { p.z = -p.z; v.z = fabsf(v.z); }
+            if (p.z > P.lz) { p.z = 2.f * P.lz - p.z; v.z = -fabsf(v.z); }
+            if (P.surface_flux && surf && p.z < P.dz) {
+                const float Pi = powf(fmaxf(snd_eval(P.snd_p, P.snd_n, p.z).v(), 1.f) / P0, R_D / CP);
+                const float Ta = t.x * Pi;
+                t.x += P.c_h * P.v_bg * (s_Ts - Ta) * dt / P.dz;
+                t.y += P.beta_moist * P.c_e * P.v_bg * (s_qs - t.y) * dt / P.dz;
+                t.x = fminf(fmaxf(t.x, 100.f), P.theta_cap);
+                t.y = fminf(fmaxf(t.y, 0.f), P.qv_cap);
             }
+            if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v.x) && isfinite(v.y) &&
+                  isfinite(v.z)))
+                stop_run(ctl, ASPH_ERR_NONFINITE);
         }
-        const float4 a = A.acc[P.permute_acc ? s : i];
-        const float hdt = 0.5f * dt;
-        v.x += a.x * hdt; v.y += a.y * hdt; v.z += a.z * hdt;
-        p.x += v.x * dt; p.y += v.y * dt; p.z += v.z * dt;
-        for (int k = 0; k < 64 && p.x < 0.f; ++k) p.x += P.lx;
-        for (int k = 0; k < 64 && p.x >= P.lx; ++k) p.x -= P.lx;
-        for (int k = 0; k < 64 && p.y < 0.f; ++k) p.y += P.ly;
-        for (int k = 0; k < 64 && p.y >= P.ly; ++k) p.y -= P.ly;
-        if (p.z < 0.f) { p.z = -p.z; v.z = fabsf(v.z); }
-        if (p.z > P.lz) { p.z = 2.f * P.lz - p.z; v.z = -fabsf(v.z); }
-        if (P.surface_flux && surf && p.z < P.dz) {
-            const float Pi = powf(fmaxf(snd_eval(P.snd_p, P.snd_n, p.z).v(), 1.f) / P0, R_D / CP);
-            const float Ta = t.x * Pi;
-            t.x += P.c_h * P.v_bg * (s_Ts - Ta) * dt / P.dz;
-            t.y += P.beta_moist * P.c_e * P.v_bg * (s_qs - t.y) * dt / P.dz;
-            t.x = fminf(fmaxf(t.x, 100.f), P.theta_cap);
-            t.y = fminf(fmaxf(t.y, 0.f), P.qv_cap);
-        }
+        A.pos_dst[i] = make_float4(p.x, p.y, p.z, rho);
+        A.vel_dst[i] = v;
+        A.thq_dst[i] = t;
+        A.kin[i] = key_of(P, p.x, p.y, p.z);
     }
-    A.pos_dst[i] = make_float4(p.x, p.y, p.z, rho);
-    A.vel_dst[i] = v;
-    A.thq_dst[i] = t;
-    A.kin[i] = key_of(P, p.x, p.y, p.z);
 }
 
 // Standalone rain pass (granular API).

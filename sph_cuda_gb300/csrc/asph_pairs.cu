@@ -92,20 +92,38 @@ __device__ __forceinline__ int block_excl_scan_int(int v, int* s_warp, int* tota
 }
 
 // Walk the reference window of one target through the global cell table.
+// At most ASPH_MAX_CANDIDATES candidates are visited: a denser window can
+// only come from a blown-up state (the reference would spend quadratic
+// time on it), so the run is stopped with ASPH_ERR_DENSE instead.
 template <class F>
-__device__ __forceinline__ void for_window_global(const Phys& P, const int2* __restrict__ range, float x, float y,
-                                                  float z, F&& f) {
+__device__ __forceinline__ void for_window_global(const Phys& P, const int2* __restrict__ range, DevCtl* ctl, float x,
+                                                  float y, float z, F&& f) {
     const int ix = cell_ix(x, P.inv_dx, P.nx), iy = cell_ix(y, P.inv_dy, P.ny), iz = cell_ix(z, P.inv_dz, P.nz);
     const int z0 = max(iz - STENCIL, 0), z1 = min(iz + STENCIL, P.nz - 1);
+    int budget = ASPH_MAX_CANDIDATES;
     for (int jz = z0; jz <= z1; ++jz)
         for (int jy = iy - STENCIL; jy <= iy + STENCIL; ++jy) {
             const int cy = wrapi(jy, P.ny);
             const int2* row = range + (size_t)(jz * P.ny + cy) * P.nx;
             for (int jx = ix - STENCIL; jx <= ix + STENCIL; ++jx) {
                 const int2 rg = row[wrapi(jx, P.nx)];
+                budget -= rg.y - rg.x;
+                if (budget < 0) {
+                    stop_run(ctl, ASPH_ERR_DENSE);
+                    return;
+                }
                 for (int j = rg.x; j < rg.y; ++j) f(j);
             }
         }
+}
+
+// Span of one window row (cells ix-2 .. ix+2) inside the staged region.
+// (Culling the span geometrically with a drift bound was measured slower at
+// 0.6 particles per cell: the per-row arithmetic costs more than the candidates it
+// removes.)
+__device__ __forceinline__ void row_span(const int* s_off, int la_m2, int& k, int& kend) {
+    k = s_off[la_m2];
+    kend = s_off[la_m2 + 2 * STENCIL + 1];
 }
 
 // Region-local window of a target: returns false if it leaves the region.
@@ -180,10 +198,10 @@ struct DArgs {
 
 // Out of line: only targets that leave the staged region come here, and
 // keeping it out of the brick kernel keeps that kernel free of spills.
-__device__ __noinline__ void density_target_global(const Phys& P, const DArgs& A, int i, float4 pi, DSum& s,
-                                                    const FF& rr) {
+__device__ __noinline__ DSum density_target_global(const Phys& P, const DArgs& A, int i, float4 pi, FF rr) {
+    DSum s{0.f, 0.f, 0.f};
     NbrOut L{A.nbr, 0, P.N, i};
-    for_window_global(P, A.range, pi.x, pi.y, pi.z, [&](int j) {
+    for_window_global(P, A.range, A.ctl, pi.x, pi.y, pi.z, [&](int j) {
         const float4 pj = A.pos[j];
         const float r2 = r2_cells(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z);
         if (r2 < 4.0f) {
@@ -192,6 +210,7 @@ __device__ __noinline__ void density_target_global(const Phys& P, const DArgs& A
         }
     });
     A.nbr_cnt[i] = L.n <= NBR_CAP ? L.n : -1;
+    return s;
 }
 
 __global__ __launch_bounds__(256) void k_density_global(const __grid_constant__ Phys P,
@@ -201,8 +220,7 @@ __global__ __launch_bounds__(256) void k_density_global(const __grid_constant__ 
     const float dt = A.ctl->dt;
     const float4 pi = A.pos[i];
     const FF rr = snd_eval(P.snd_rho, P.snd_n, pi.z);
-    DSum s{0.f, 0.f, 0.f};
-    density_target_global(P, A, i, pi, s, rr);
+    const DSum s = density_target_global(P, A, i, pi, rr);
     density_eos_epilogue(P, A.out, i, pi, s, rr, dt);
 }
 
@@ -304,36 +322,35 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
         }                                                                             \
         n = 0;                                                                        \
     } while (0)
-        // flattened walk of the window rows in the staged region
+        // flattened walk of the window rows in the staged region; the warp
+        // votes once per 4 steps, so queues drain at DLIST - 4
         bool done = !fast;
         int jz = zlo, jy = ly - STENCIL, k = 0, kend = 0;
-        if (!done) {
-            const int la = (jz * G::RY + jy) * G::RX + lx - STENCIL;
-            k = s_off[la];
-            kend = s_off[la + 5];
-        }
+        if (!done) row_span(s_off, (jz * G::RY + jy) * G::RX + lx - STENCIL, k, kend);
         for (;;) {
-            if (!done) {
-                if (k < kend) {
-                    const float4 pj = sp[k];
-                    if (r2_cells(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z) < 4.0f) s_list[(n++) * T + threadIdx.x] = (unsigned short)k;
-                    ++k;
-                } else if (++jy > ly + STENCIL && (jy = ly - STENCIL, ++jz > zhi)) {
-                    done = true;
-                } else {
-                    const int la = (jz * G::RY + jy) * G::RX + lx - STENCIL;
-                    k = s_off[la];
-                    kend = s_off[la + 5];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (!done) {
+                    if (k < kend) {
+                        const float4 pj = sp[k];
+                        if (r2_cells(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z) < 4.0f)
+                            s_list[(n++) * T + threadIdx.x] = (unsigned short)k;
+                        ++k;
+                    } else if (++jy > ly + STENCIL && (jy = ly - STENCIL, ++jz > zhi)) {
+                        done = true;
+                    } else {
+                        row_span(s_off, (jz * G::RY + jy) * G::RX + lx - STENCIL, k, kend);
+                    }
                 }
             }
-            if (__any_sync(0xffffffffu, n == DLIST)) ASPH_DRAIN();
+            if (__any_sync(0xffffffffu, n > DLIST - 4)) ASPH_DRAIN();
             if (__all_sync(0xffffffffu, done)) break;
         }
         ASPH_DRAIN();
 #undef ASPH_DRAIN
         if (active) {
             if (fast) A.nbr_cnt[i] = L.n <= NBR_CAP ? L.n : -1;
-            else density_target_global(P, A, i, pi, s, rr);
+            else s = density_target_global(P, A, i, pi, rr);
             density_eos_epilogue(P, A.out, i, pi, s, rr, dt);
         }
     }
@@ -358,6 +375,20 @@ struct MArgs {
     DevCtl* ctl;
     int part_blocks;       // blocks of particle work; the rest advect rain
 };
+
+// Out of line: targets without a usable neighbour list come here.
+__device__ __noinline__ MSum momentum_target_global(const Phys& P, const MArgs& A, const MTarget T) {
+    MSum s{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for_window_global(P, A.range, A.ctl, T.x, T.y, T.z, [&](int j) {
+        const float4 pj = A.pos[j];
+        const float r2t = r2_cells(P, T.x, T.y, T.z, pj.x, pj.y, pj.z);
+        if (r2t >= 4.0f || r2t < 1e-12f) return;   // also excludes j == i
+        const float2 rj = A.rp[j];
+        const float4 vj = A.vel[j];
+        msum_add(P, s, T, make_float4(pj.x, pj.y, pj.z, rj.y), make_float4(vj.x, vj.y, vj.z, rj.x));
+    });
+    return s;
+}
 
 __global__ __launch_bounds__(M_TPB) void k_momentum(const __grid_constant__ Phys P, const __grid_constant__ MArgs A,
                                                     int mode) {
@@ -388,7 +419,26 @@ __global__ __launch_bounds__(M_TPB) void k_momentum(const __grid_constant__ Phys
                 MSum s{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 const int cnt = A.use_lists ? A.nbr_cnt[i] : -1;
                 if (cnt >= 0) {
-                    for (int q = 0; q < cnt; ++q) {
+                    // four neighbours' loads in flight before their arithmetic
+                    int q = 0;
+                    for (; q + 4 <= cnt; q += 4) {
+                        int jj[4];
+                        float4 pp[4], vv[4];
+                        float2 rr[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) jj[u] = A.nbr[(size_t)(q + u) * P.N + i];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            pp[u] = A.pos[jj[u]];
+                            rr[u] = A.rp[jj[u]];
+                            vv[u] = A.vel[jj[u]];
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            msum_add(P, s, T, make_float4(pp[u].x, pp[u].y, pp[u].z, rr[u].y),
+                                     make_float4(vv[u].x, vv[u].y, vv[u].z, rr[u].x));
+                    }
+                    for (; q < cnt; ++q) {
                         const int j = A.nbr[(size_t)q * P.N + i];
                         const float4 pj = A.pos[j];
                         const float2 rj = A.rp[j];
@@ -396,14 +446,7 @@ __global__ __launch_bounds__(M_TPB) void k_momentum(const __grid_constant__ Phys
                         msum_add(P, s, T, make_float4(pj.x, pj.y, pj.z, rj.y), make_float4(vj.x, vj.y, vj.z, rj.x));
                     }
                 } else {
-                    for_window_global(P, A.range, T.x, T.y, T.z, [&](int j) {
-                        const float4 pj = A.pos[j];
-                        const float r2t = r2_cells(P, T.x, T.y, T.z, pj.x, pj.y, pj.z);
-                        if (r2t >= 4.0f || r2t < 1e-12f) return;   // also excludes j == i
-                        const float2 rj = A.rp[j];
-                        const float4 vj = A.vel[j];
-                        msum_add(P, s, T, make_float4(pj.x, pj.y, pj.z, rj.y), make_float4(vj.x, vj.y, vj.z, rj.x));
-                    });
+                    s = momentum_target_global(P, A, T);
                 }
                 m = momentum_epilogue(P, A.out, i, T, s, (mode & M_INTEGRATE) != 0, dt);
             }

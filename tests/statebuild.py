@@ -7,8 +7,8 @@ from sph_cuda_gb300 import preset
 
 def small_config(lat=(16, 16, 16), grid=(20, 20, 40), box=(4000.0, 4000.0, 2000.0), **kw):
     """Config-mode physics (4 K/km, RH profile, warm rain with accretion and
-    evaporation) on a small box: same cell aspect as cfg0 (200 m x 50 m)."""
-    p = preset("cfg0")
+    evaporation) on a small box: the 200 m x 50 m cells of the 65,536-particle preset."""
+    p = preset("small65k")
     p.nx, p.ny, p.nz = grid
     p.dx, p.dy, p.dz = box[0] / grid[0], box[1] / grid[1], box[2] / grid[2]
     p.lat_nx, p.lat_ny, p.lat_nz = lat

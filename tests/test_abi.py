@@ -33,7 +33,7 @@ def test_layout_and_version():
     assert lib.asph_status_string(3) == b"CFL trip limit exceeded"
 
 
-@pytest.mark.parametrize("name", ["reference", "cfg0", "cfg1", "cfg2", "cfg3"])
+@pytest.mark.parametrize("name", ["reference", "small65k", "bubble2m", "large16m", "adjoint262k"])
 def test_presets_are_valid(name):
     p = preset(name, 16, 16, 8) if name == "reference" else preset(name)
     check_params(p)
@@ -41,8 +41,8 @@ def test_presets_are_valid(name):
     assert d["pmass"] > 0 and d["dt_cap"] <= d["dt_static"] + 1e-12
 
 
-def test_cfg1_geometry():
-    p = preset("cfg1")
+def test_bubble2m_geometry():
+    p = preset("bubble2m")
     assert (p.nx, p.ny, p.nz) == (133, 133, 200)
     assert p.n_particles == 128 ** 3 == 2097152
     assert abs(p.dx - 20000.0 / 133) < 1e-3 and p.dz == 40.0
@@ -73,7 +73,7 @@ def test_morton_limit_rejected():
 
 
 def test_bad_lattice_rejected():
-    p = preset("cfg0")
+    p = preset("small65k")
     p.lat_nx = 31
     with pytest.raises(AsphError):
         check_params(p)

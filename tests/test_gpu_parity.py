@@ -101,10 +101,10 @@ def test_sort_sorted_and_reversed_input():
     _check_sort(p, rev)
 
 
-def test_sort_full_size_cfg1_bit_exact():
+def test_sort_full_size_2m_bit_exact():
     p = small_config()
     from sph_cuda_gb300 import preset
-    p = preset("cfg1")
+    p = preset("bubble2m")
     s = random_state(p, 11, "uniform")
     _check_sort(p, s)
 
@@ -384,3 +384,89 @@ def test_dump_matches_host_means(tmp_path):
             cnt[iz // 3, iy // 10, ix // 10] += 1
     means /= np.maximum(cnt, 1)[..., None]
     assert np.allclose(d["data"], means, rtol=1e-5, atol=1e-6)
+
+
+# ---------------------------------------------------------------------------
+# neighbour lists: the culled brick path accepts exactly the reference's pairs
+# ---------------------------------------------------------------------------
+def _lists_after_density(p, s, global_path):
+    sim = _ctx(p, s)
+    sim.set_pair_path(global_path)
+    sim.sort_build()
+    sim.kick_drift_flux()
+    st = sim.get_state(("x", "y", "z"))
+    cr = sim.get_sort()["cell_range"]
+    sim.density_eos()
+    cnt, lst = sim.neighbours()
+    sim.close()
+    sets = [np.sort(lst[:c, i]) for i, c in enumerate(cnt)]
+    return st, cr, cnt, sets
+
+
+def _window_rule(p, st, cr, i):
+    """Neighbours of i by the reference's rule (asph_h100.cu:296-327), in
+    float32, with the r2 of each pair."""
+    f32 = np.float32
+    inv = [f32(1) / f32(p.dx), f32(1) / f32(p.dy), f32(1) / f32(p.dz)]
+    pos = [st["x"], st["y"], st["z"]]
+    n = [p.nx, p.ny, p.nz]
+    c = [min(max(int(f32(pos[a][i]) * inv[a]), 0), n[a] - 1) for a in range(3)]
+    out = {}
+    for jz in range(max(c[2] - 2, 0), min(c[2] + 2, p.nz - 1) + 1):
+        for jy in range(c[1] - 2, c[1] + 3):
+            for jx in range(c[0] - 2, c[0] + 3):
+                cid = (jz * p.ny + jy % p.ny) * p.nx + jx % p.nx
+                a, b = cr[cid]
+                for j in range(a, b):
+                    d = [(pos[k][i] - pos[k][j]) * inv[k] for k in range(3)]
+                    r2 = f32(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+                    if r2 < 4.0 and r2 >= 1e-12:
+                        out[j] = float(r2)
+    return out
+
+
+@pytest.mark.parametrize("name", ["cfg_jitter", "ref_fast", "cfg_wide"])
+def test_neighbour_lists_exact(name):
+    p, s = _case(name)
+    st_b, cr, cnt_b, sets_b = _lists_after_density(p, s, False)
+    st_g, _, cnt_g, sets_g = _lists_after_density(p, s, True)
+    assert np.array_equal(st_b["x"], st_g["x"])
+    assert np.array_equal(cnt_b, cnt_g)
+    for i in range(p.n_particles):
+        assert np.array_equal(sets_b[i], sets_g[i]), i
+    # the window rule in float32 on a sample of targets
+    rng = np.random.default_rng(0)
+    for i in rng.choice(p.n_particles, size=min(300, p.n_particles), replace=False):
+        ref = _window_rule(p, st_b, cr, i)
+        got = set(sets_b[i].tolist())
+        for j, r2 in ref.items():
+            assert j in got or abs(r2 - 4.0) < 1e-4, (i, j, r2)
+        for j in got:
+            assert j in ref, (i, j)
+
+
+# ---------------------------------------------------------------------------
+# runaway guards: a blown-up state stops the run instead of searching forever
+# ---------------------------------------------------------------------------
+def test_nonfinite_state_stops_run():
+    p, s = _case("cfg_jitter")
+    s = {k: v.copy() for k, v in s.items()}
+    s["w"][17] = np.nan
+    sim = _ctx(p, s)
+    with pytest.raises(AsphError) as e:
+        sim.step(3)
+    assert e.value.status == abi.ASPH_ERR_NONFINITE
+    c = sim.control()
+    assert c["aborted"] == 1 and c["step"] <= 1
+    sim.close()
+
+
+def test_dense_window_stops_run():
+    p = small_config(lat=(48, 48, 32))          # 73,728 particles
+    s = random_state(p, 13, "onecell")          # all in one cell: > ASPH_MAX_CANDIDATES per window
+    sim = _ctx(p, s)
+    with pytest.raises(AsphError) as e:
+        sim.step(2)
+    assert e.value.status == abi.ASPH_ERR_DENSE
+    assert sim.control()["aborted"] == 1
+    sim.close()

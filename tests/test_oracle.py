@@ -56,7 +56,7 @@ def _np_keys(p, x, y, z):
 
 
 def test_keys_sort_table_properties():
-    p = preset("cfg0")
+    p = preset("small65k")
     rng = np.random.default_rng(3)
     N = p.n_particles
     x = rng.uniform(0, p.nx * p.dx, N).astype(np.float32)
