@@ -102,6 +102,20 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def job_rate(units: float, seconds_local: float, dist=None, device="cpu"):
+    """Whole-job throughput of independent replicas: every rank processes
+    `units` inside its own timed region and the job time is the maximum over
+    ranks.  Returns (units/s over all ranks, job seconds)."""
+    import torch
+    t = torch.tensor([seconds_local], dtype=torch.float64, device=device)
+    ws = 1
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ws = dist.get_world_size()
+    sec = float(t.item())
+    return ws * units / sec, sec
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -138,29 +152,54 @@ def oracle_initial_state(p):
     return oracle.init_state(p)
 
 
+def workload_string(name: str) -> str:
+    return {"bubble2m": "moist bubble, 2,097,152 particles, 133x133x200 cells, sort every step",
+            "bubble524k": "moist bubble, 524,288 particles, 66x66x200 cells, sort every step"}[name]
+
+
 def run_reference(args):
+    """The reference's CPU path (the FP64 oracle port, all host threads) on a
+    bounded sample of the workload: each step is one full step of the
+    131,072-particle box with the workload's cells and physics."""
     ws, rank, local = dist_setup()
     if rank != 0:
         return 0
     from oracle import oracle
     p = cpu_sample_params()
     state = oracle_initial_state(p)
-    # one warm-up step, then K timed steps, each one full FP64 step of the sample
-    oracle.run(p, state, 1)
+    oracle.run(p, state, max(args.warmup, 1))   # warm-up: page in, thread pool
     t, cores, _ = time_oracle(p, state, args.steps)
     value = p.n_particles * args.steps / t
+    sample = ("%d consecutive FP64 steps of the 131,072-particle moist-bubble box "
+              "(same cells and physics, 5 x 5 km footprint)" % args.steps)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": "moist bubble (sample: 131,072-particle quarter box)",
-                                       "particles": p.n_particles, "cells": p.nx * p.ny * p.nz},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "%d full FP64 steps of the 131,072-particle quarter-box moist-bubble sample" % args.steps},
+        "data": "synthetic",
+        "config": {"workload": workload_string(args.workload), "sample": sample,
+                   "sample_particles": p.n_particles, "sample_cells": p.nx * p.ny * p.nz},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
+
+
+def workload_params(name: str):
+    """bubble2m: the headline 2,097,152-particle moist-bubble workload.
+    bubble524k: the same physics, cell size and density on a 10 x 10 x 8 km box
+    (64 x 64 x 128 lattice, 66 x 66 x 200 cells) for profiler captures."""
+    import sph_cuda_gb300 as sph
+    p = sph.preset("bubble2m")
+    if name == "bubble524k":
+        p.nx = p.ny = 66
+        p.lat_nx = p.lat_ny = 64
+        p.n_particles = 64 * 64 * 128
+        for b in range(p.n_bubbles):
+            p.bubble_x[b] *= 66 / 133.0
+            p.bubble_y[b] *= 66 / 133.0
+    return p
 
 
 def run_ours(args):
@@ -174,7 +213,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     stream = torch.cuda.Stream()
-    p = sph.preset("bubble2m")
+    p = workload_params(args.workload)
     N, C = p.n_particles, p.nx * p.ny * p.nz
     sim = sph.Asph(p, stream=stream.cuda_stream)
     sim.init()
@@ -202,12 +241,8 @@ def run_ours(args):
     sim.sync()
     clk = clocks.stop()
     barrier()
-    ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t.item())
-    value = ws * N * args.steps / (ms / 1e3)
+    value, sec = job_rate(N * args.steps, e0.elapsed_time(e1) / 1e3, dist, "cuda")
+    ms = sec * 1e3
 
     # per-kernel device times of the same step (non-graph launches, events
     # between the kernels on the simulation stream)
@@ -220,7 +255,7 @@ def run_ours(args):
     hbm, src = peaks()
     achieved = algo[dom] / (ph_ms[dom] / 1e3) / 1e9
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic_bubble2m.json.txt")
+    tfile = os.path.join(ROOT, "profiles", "traffic_%s.txt" % args.workload)
     if os.path.exists(tfile):
         try:
             traffic = json.load(open(tfile)).get(dom)
@@ -239,21 +274,21 @@ def run_ours(args):
         sim.set_state(host)
         sim.step(1)
         sim.get_state(fields, out=host)
-    t_e2e = time.perf_counter() - t0
-    tt = torch.tensor([t_e2e], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-    e2e = ws * N * e2e_steps / float(tt.item())
+    e2e, _ = job_rate(N * e2e_steps, time.perf_counter() - t0, dist, "cuda")
     nbytes = len(fields) * 4 * N
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         ps = cpu_sample_params()
         st = oracle_initial_state(ps)
-        tc, cores, _ = time_oracle(ps, st, args.cpu_steps)
-        cpu = {"value": ps.n_particles * args.cpu_steps / tc, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": "%d full FP64 steps of the 131,072-particle quarter-box moist-bubble sample (%.1f s)"
-                         % (args.cpu_steps, tc)}
+        nsteps = args.cpu_steps
+        if nsteps <= 0:   # size the sample to about 12 s of CPU work
+            t1, _, _ = time_oracle(ps, st, 1)
+            nsteps = int(min(400, max(3, round(12.0 / max(t1, 1e-3)))))
+        tc, cores, _ = time_oracle(ps, st, nsteps)
+        cpu = {"value": ps.n_particles * nsteps / tc, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "%d consecutive FP64 steps of the 131,072-particle moist-bubble box "
+                         "(same cells and physics, 5 x 5 km footprint) in %.1f s" % (nsteps, tc)}
 
     ctl = sim.control()
     if rank == 0:
@@ -261,7 +296,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "moist bubble, 2,097,152 particles, 133x133x200 cells, sort every step",
+            "config": {"workload": workload_string(args.workload),
                        "particles": N, "cells": C, "dt_s": ctl["dt"],
                        "l2": "working set %.0f MB > 129 MB L2 (no flush needed)" % ((N * 164 + C * 20) / 1e6),
                        "parallelism": "replicas x%d" % ws},
@@ -284,17 +319,22 @@ def run_ours(args):
     return 0
 
 
-def main():
+def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=0, help="0: about 12 s of oracle steps")
     ap.add_argument("--no-cpu", action="store_true")
-    args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    ap.add_argument("--workload", default="bubble2m", choices=["bubble2m", "bubble524k"])
+    args = ap.parse_args(argv)
+    args.warmup = max(args.warmup, 3)
+    return args
+
+
+def main():
+    args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

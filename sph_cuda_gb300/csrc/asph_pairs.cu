@@ -35,7 +35,7 @@
 namespace asph {
 
 constexpr int HALO = 3;
-constexpr int DLIST = 16;        // queued accepted candidates per thread (D)
+constexpr int DLIST = 24;        // queued accepted candidates per thread (D)
 constexpr int M_TPB = 256;
 
 template <int BX, int BY, int BZ>

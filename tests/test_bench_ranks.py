@@ -1,0 +1,79 @@
+"""Multi-process host logic of bench.py on CPU (gloo, world size 2).
+
+The path does not shard: N GPUs run N independent replicas, and the job
+rate is all units over the slowest rank's time.  The reference arm runs on
+rank 0 only; the other ranks exit 0 without output.
+"""
+import io
+import os
+import socket
+import sys
+from contextlib import redirect_stdout
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, units, seconds, out):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        rate, sec = bench.job_rate(units, seconds[rank], dist, "cpu")
+        out.put((rank, rate, sec))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_job_rate_single():
+    rate, sec = bench.job_rate(1000.0, 2.0)
+    assert sec == 2.0 and rate == 500.0
+
+
+def test_job_rate_two_ranks_takes_slowest():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    units, seconds = 4.0e6, [0.5, 0.8]
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, units, seconds, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, rate, sec in res:
+        assert sec == pytest.approx(0.8)
+        assert rate == pytest.approx(2 * units / 0.8)
+
+
+def test_reference_arm_nonzero_rank_is_silent(monkeypatch):
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    monkeypatch.setenv("RANK", "1")
+    monkeypatch.setenv("LOCAL_RANK", "1")
+    args = bench.parse_args(["--impl", "reference", "--gpus", "2", "--steps", "3", "--warmup", "3"])
+    buf = io.StringIO()
+    with redirect_stdout(buf):
+        rc = bench.run_reference(args)
+    assert rc == 0 and buf.getvalue() == ""
+
+
+def test_workload_presets_match_their_descriptions():
+    p = bench.workload_params("bubble2m")
+    assert p.n_particles == 2097152 and (p.nx, p.ny, p.nz) == (133, 133, 200)
+    q = bench.workload_params("bubble524k")
+    assert q.n_particles == 524288 and (q.nx, q.ny, q.nz) == (66, 66, 200)
+    assert q.dx == pytest.approx(p.dx) and q.dz == pytest.approx(p.dz)
+    s = bench.cpu_sample_params()
+    assert s.n_particles == 131072 and s.dx == pytest.approx(p.dx)
