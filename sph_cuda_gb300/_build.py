@@ -72,8 +72,10 @@ def build_cli(force: bool = False) -> str:
     if not os.path.exists(src):
         return ""
     if force or _stale(CLI, [src, LIB, os.path.join(ROOT, "include", "asph.h")]):
-        _run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-o", CLI,
-              "-L", BUILD, "-lasph", "-Wl,-rpath,$ORIGIN"])
+        cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"),
+              "-I", os.path.join(cuda, "include"), src, "-o", CLI,
+              "-L", BUILD, "-lasph", "-L", os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN"])
     return CLI
 
 

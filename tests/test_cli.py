@@ -1,0 +1,87 @@
+"""The command-line driver (the reference's executable boundary).
+
+CPU: flag parsing, --help, the Morton grid limit and bad flags give the
+reference's exit codes without touching a GPU.  GPU: a short run writes the
+reference's dump files, and its dumps are byte-identical to dumps taken
+through the library API after the same number of steps.
+"""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from sph_cuda_gb300 import Asph, preset, _build
+from sph_cuda_gb300 import dumpfmt
+
+
+@pytest.fixture(scope="module")
+def cli():
+    path = _build.build_cli()
+    assert path and os.path.exists(path)
+    return path
+
+
+def _run(cli, *args, cwd=None, timeout=600):
+    return subprocess.run([cli, *map(str, args)], capture_output=True, text=True, cwd=cwd, timeout=timeout)
+
+
+def test_help(cli):
+    r = _run(cli, "--help")
+    assert r.returncode == 0
+    for flag in ("--nx", "--dt", "--cfl", "--cfl-interval", "--max-trip", "--strict-cfl", "--dump-every",
+                 "--sim-hours", "--dump-stride", "--outdir", "--noise", "--validate", "--quick"):
+        assert flag in r.stdout
+
+
+def test_morton_limit_exits_1(cli):
+    r = _run(cli, "--nx", 2000)
+    assert r.returncode == 1
+    assert "1024 cells/axis" in r.stderr
+
+
+@pytest.mark.parametrize("args", [["--nx"], ["--dump-stride", "3"], ["--bogus", "1"], ["--preset", "nope"], ["x"]])
+def test_bad_arguments_exit_1(cli, args):
+    r = _run(cli, *args)
+    assert r.returncode == 1
+    assert "ERROR" in r.stderr
+
+
+def test_grid_too_small_is_a_config_error(cli):
+    r = _run(cli, "--nx", 2, "--ny", 8, "--nz", 8)
+    assert r.returncode == 1
+    assert "invalid configuration" in r.stderr
+
+
+DUMP_LINE = re.compile(r"^(\d+)\s+\+(\d+)\s*s\s+\S+\s+(\S+)\s+CFL")
+
+
+@pytest.mark.gpu
+def test_cli_dumps_match_library(cli, tmp_path):
+    out = tmp_path / "dumps"
+    r = _run(cli, "--nx", 16, "--ny", 16, "--nz", 16, "--dump-every", 30, "--sim-hours", 0.02, "--validate",
+             "--dump-stride", 4, 4, "--outdir", out, "--report", 50)
+    assert r.returncode == 0, r.stderr
+    assert "=== DONE" in r.stdout and "AUDIT" in r.stdout and "DRIFT" in r.stdout
+    lines = [DUMP_LINE.match(l) for l in r.stdout.splitlines()]
+    dumps = [(int(m.group(1)), int(m.group(2))) for m in lines if m]
+    files = sorted(os.listdir(out))
+    assert len(dumps) == 2 and len(files) == 2
+    # the same run through the library: the dump after the same step count is identical
+    p = preset("reference", 16, 16, 16)
+    p.dump_sx = p.dump_sy = 4
+    p.dump_sz = 4
+    sim = Asph(p)
+    sim.init()
+    done = 0
+    for (step, t), fn in zip(dumps, files):
+        assert fn == "asph_t%06ds.bin" % t
+        sim.step(step - done)
+        done = step
+        mine = sim.dump(str(tmp_path / "lib"))
+        assert os.path.basename(mine) == fn
+        assert open(out / fn, "rb").read() == open(mine, "rb").read()
+        d = dumpfmt.read(str(out / fn))
+        assert (d["nx"], d["cx"], d["cz"], d["sx"], d["sz"]) == (16, 4, 4, 4, 4)
+    sim.close()
