@@ -102,6 +102,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def launches_per_step(p) -> int:
+    """Kernels of one step: sort preparation, histogram, one radix pass per
+    8 key bits (3 bits per level of the largest axis), gather, density,
+    momentum."""
+    bits = 1
+    while (1 << bits) < max(p.nx, p.ny, p.nz):
+        bits += 1
+    return 5 + (3 * bits + 7) // 8
+
+
 def job_rate(units: float, seconds_local: float, dist=None, device="cpu"):
     """Whole-job throughput of independent replicas: every rank processes
     `units` inside its own timed region and the job time is the maximum over
@@ -217,11 +227,7 @@ def run_ours(args):
     N, C = p.n_particles, p.nx * p.ny * p.nz
     sim = sph.Asph(p, stream=stream.cuda_stream)
     sim.init()
-    bits = 1
-    while (1 << bits) < max(p.nx, p.ny, p.nz):
-        bits += 1
-    npasses = (3 * bits + 7) // 8
-    launches_per_step = 5 + npasses   # table clear, histogram, passes, gather, density, momentum
+    per_step = launches_per_step(p)
     sim.step(max(args.warmup, 1))
 
     def barrier():
@@ -307,7 +313,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "steps": e2e_steps, "api": "asph_set_state + asph_step(1) + asph_get_state, pinned host SoA"},
-            "gpu_launches": launches_per_step * args.steps,
+            "gpu_launches": per_step * args.steps,
             "clocks": clk,
             "state": {"simt": ctl["simt"], "steps_done": ctl["step"], "aborted": ctl["aborted"],
                       "wmax": ctl["wmax"]},
@@ -319,6 +325,70 @@ def run_ours(args):
     return 0
 
 
+def run_ensemble(args):
+    """64 members of uneven size stepped together (one graph launch per
+    ensemble step) against the same members stepped one after another
+    through the plain step, with the same tuned options."""
+    import torch
+    import sph_cuda_gb300 as sph
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    members = sph.ensemble_members(64, seed=7)
+    total = sum(int(p.n_particles) for p in members)
+    ens = sph.Ensemble(members, stream=stream.cuda_stream)
+    ens.init()
+    t0 = time.perf_counter()
+    chosen = ens.tune(trial_steps=3, sort_choices=(0, 1, 2)) if not args.no_tune else []
+    t_tune = time.perf_counter() - t0
+    ens.step(args.warmup)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    e0.record(stream)
+    ens.step_async(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ens.sync()
+    clk = clocks.stop()
+    ms_ens = e0.elapsed_time(e1)
+    # the same members one after another, each through its own captured plain step
+    views = [ens.member(k) for k in range(len(members))]
+    for v in views:
+        v.step(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for v in views:
+        v.step_async(args.steps)
+    for v in views:
+        v.sync()
+    ms_seq = (time.perf_counter() - t0) * 1e3
+    line = {
+        "metric": "aggregate particle-steps/s (64-member ensemble)", "value": total * args.steps / (ms_ens / 1e3),
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_ens / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "ensemble of 64 members, particle counts log-uniform in [16384, 524288] (seed 7), "
+                               "small-box atmosphere at fixed spacing, theta noise 0.1 K",
+                   "members": len(members), "particles_total": total,
+                   "particles_min": min(int(p.n_particles) for p in members),
+                   "particles_max": max(int(p.n_particles) for p in members)},
+        "sequential": {"value": total * args.steps / (ms_seq / 1e3), "ms_per_step": ms_seq / args.steps,
+                       "how": "each member's own graph-launched plain step, members one after another"},
+        "speedup_vs_sequential": ms_seq / ms_ens,
+        "tuning": {"seconds": t_tune, "chosen_shape_counts": {str(s): sum(1 for c in chosen if c[0] == s)
+                                                               for s in sorted(set(c[0] for c in chosen))},
+                   "chosen_sort_counts": {str(s): sum(1 for c in chosen if c[1] == s)
+                                          for s in sorted(set(c[1] for c in chosen))}},
+        "gpu_launches": args.steps * sum(launches_per_step(p) for p in members),
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    ens.close()
+    return 0
+
+
 def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -327,7 +397,8 @@ def parse_args(argv=None):
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=0, help="0: about 12 s of oracle steps")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="bubble2m", choices=["bubble2m", "bubble524k"])
+    ap.add_argument("--workload", default="bubble2m", choices=["bubble2m", "bubble524k", "ensemble64"])
+    ap.add_argument("--no-tune", action="store_true", help="ensemble64: skip the autotuner")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     return args
@@ -337,6 +408,8 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "ensemble64":
+        return run_ensemble(args)
     return run_ours(args)
 
 

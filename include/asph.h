@@ -211,12 +211,19 @@ int asph_sync(asph_ctx* ctx);
 #define ASPH_NPHASES 6
 int asph_step_profiled(asph_ctx* ctx, int nsteps, float* phase_ms);
 
-/* Execution options.  ASPH_OPT_PAIR_PATH: 0 = automatic (brick-staged
- * shared-memory pair kernels where the grid allows), 1 = per-target global
- * path everywhere (same results; for testing).  ASPH_OPT_PAIR_SHAPE (get
- * only): index of the brick shape in use, -1 for the global path. */
+/* Execution options (setting one drops the captured step graphs).
+ * ASPH_OPT_PAIR_PATH: 0 = automatic (brick-staged shared-memory pair
+ * kernels where the grid allows), 1 = per-target global path everywhere
+ * (same results to rounding; for testing).
+ * ASPH_OPT_PAIR_SHAPE: brick shape of the density pass, 0 = 8x8x8,
+ * 1 = 8x8x4, 2 = 8x4x4, 3 = 4x4x4 cells, -1 = automatic (set); get returns
+ * the shape in use, -1 for the global path.  A shape whose staged region
+ * does not suit the grid or the particle density is ASPH_ERR_ARG.
+ * ASPH_OPT_SORT_EVERY: sort cadence, 0 = displacement-gated (the
+ * reference), k > 0 = every k steps (the AsphParams field sort_every). */
 #define ASPH_OPT_PAIR_PATH  1
 #define ASPH_OPT_PAIR_SHAPE 2
+#define ASPH_OPT_SORT_EVERY 3
 int asph_set_option(asph_ctx* ctx, int option, int value);
 int asph_get_option(asph_ctx* ctx, int option, int* value);
 
@@ -237,6 +244,49 @@ int asph_dump(asph_ctx* ctx, const char* outdir, char* path, int path_len);
  * cover [%], max ql [kg/kg], max |w| [m/s], mean precipitation [mm];
  * resets the precipitation accumulator like the reference. */
 int asph_column_diag(asph_ctx* ctx, float out[4]);
+
+/* ---- state snapshots and restart files -------------------------------------
+ * No counterpart in the reference (it cannot restart; its dumps are coarse
+ * averages, asph_h100.cu:680-703).  A snapshot holds, in device memory,
+ * everything a context needs to continue bit for bit: the particle field
+ * groups, the cell table and surface flags of the last sort, the rain grid,
+ * the surface precipitation and the control block.  save/restore are queued
+ * on the context's stream; a snapshot fits only contexts with its particle
+ * count and grid.  Restart files hold the same content on disk; reading one
+ * needs a context created with the same particle count and grid, whose
+ * parameters then govern the continued run. */
+typedef struct asph_snapshot asph_snapshot;
+int asph_snapshot_create(asph_ctx* ctx, asph_snapshot** out);
+int asph_snapshot_save(asph_ctx* ctx, asph_snapshot* snap);
+int asph_snapshot_restore(asph_ctx* ctx, const asph_snapshot* snap);
+int asph_snapshot_destroy(asph_snapshot* snap);
+int asph_checkpoint_write(asph_ctx* ctx, const char* path);
+int asph_checkpoint_read(asph_ctx* ctx, const char* path);
+
+/* ---- ensemble ----------------------------------------------------------------
+ * No counterpart in the reference.  n_members independent simulations of
+ * any sizes, each a full context (own parameters, dt, CFL control and sort
+ * cadence) on its own stream.  One ensemble step is one CUDA graph launch on
+ * `stream` (NULL: the ensemble's own stream) that forks into every member's
+ * step and joins; members run concurrently on the GPU.  A member's results
+ * equal those of the same parameters run alone with the same options.
+ * asph_ens_member() lends a member's context for state, audit and dump calls
+ * (ordered after the queued ensemble steps); the ensemble keeps ownership.
+ * asph_ens_tune() times every brick shape that suits each member (and the
+ * per-target path) crossed with the sort cadences in sort_choices (none:
+ * keep each member's own), trial_steps steps each from a snapshot, keeps
+ * the fastest per member and restores the member's state; chosen (may be
+ * NULL) receives per member {shape (-1: per-target path), sort cadence}. */
+typedef struct asph_ens asph_ens;
+int asph_ens_create(const AsphParams* members, int n_members, void* stream, asph_ens** out);
+int asph_ens_destroy(asph_ens* ens);
+int asph_ens_size(asph_ens* ens);
+int asph_ens_member(asph_ens* ens, int k, asph_ctx** ctx);
+int asph_ens_init(asph_ens* ens);
+int asph_ens_step(asph_ens* ens, int nsteps);
+int asph_ens_step_async(asph_ens* ens, int nsteps);
+int asph_ens_sync(asph_ens* ens);
+int asph_ens_tune(asph_ens* ens, int trial_steps, const int* sort_choices, int n_sort_choices, int* chosen);
 
 /* ---- stable key sort without allocation -----------------------------------
  * No counterpart in the reference.  For callers that must not call

@@ -20,7 +20,8 @@ import numpy as np
 from . import abi
 from .abi import (AsphControl, AsphHostState, AsphParams, STATE_FIELDS, load_library)
 
-__all__ = ["Asph", "AsphError", "AsphParams", "preset", "library", "STATE_FIELDS"]
+__all__ = ["Asph", "AsphError", "AsphParams", "Ensemble", "Snapshot", "ensemble_members", "preset", "library",
+           "STATE_FIELDS"]
 
 PRESETS = {
     "reference": abi.PRESET_REFERENCE,
@@ -70,18 +71,20 @@ def _fptr(a: np.ndarray):
 class Asph:
     """One simulation context (device buffers, stream, captured graphs)."""
 
-    def __init__(self, params: AsphParams, stream: int | None = None):
+    def __init__(self, params: AsphParams, stream: int | None = None, _borrowed=None):
         self.lib = library()
         self.params = params.copy()
         self._ctx = C.c_void_p()
-        _check(self.lib.asph_create(C.byref(self.params), C.c_void_p(stream or 0), C.byref(self._ctx)))
+        self._owner = _borrowed   # an Ensemble that owns the context, or None
+        if _borrowed is None:
+            _check(self.lib.asph_create(C.byref(self.params), C.c_void_p(stream or 0), C.byref(self._ctx)))
         self.N = int(self.params.n_particles)
         self.ncell = int(self.params.nx * self.params.ny * self.params.nz)
 
     def close(self) -> None:
-        if self._ctx:
+        if self._ctx and self._owner is None:
             self.lib.asph_destroy(self._ctx)
-            self._ctx = C.c_void_p()
+        self._ctx = C.c_void_p()
 
     def __del__(self):
         try:
@@ -206,6 +209,37 @@ class Asph:
         _check(self.lib.asph_get_option(self._ctx, abi.OPT_PAIR_SHAPE, C.byref(v)))
         return v.value
 
+    def set_pair_shape(self, shape: int) -> None:
+        """Brick shape of the density pass (0..3), -1 for automatic."""
+        _check(self.lib.asph_set_option(self._ctx, abi.OPT_PAIR_SHAPE, int(shape)))
+
+    def sort_every(self) -> int:
+        v = C.c_int()
+        _check(self.lib.asph_get_option(self._ctx, abi.OPT_SORT_EVERY, C.byref(v)))
+        return v.value
+
+    def set_sort_every(self, k: int) -> None:
+        _check(self.lib.asph_set_option(self._ctx, abi.OPT_SORT_EVERY, int(k)))
+
+    # ---- snapshots and restart files --------------------------------------------
+    def snapshot(self) -> "Snapshot":
+        """A device-resident copy of the full state (see restore)."""
+        s = Snapshot(self)
+        _check(self.lib.asph_snapshot_save(self._ctx, s._h))
+        return s
+
+    def save_snapshot(self, snap: "Snapshot") -> None:
+        _check(self.lib.asph_snapshot_save(self._ctx, snap._h))
+
+    def restore(self, snap: "Snapshot") -> None:
+        _check(self.lib.asph_snapshot_restore(self._ctx, snap._h))
+
+    def checkpoint_write(self, path: str) -> None:
+        _check(self.lib.asph_checkpoint_write(self._ctx, str(path).encode()))
+
+    def checkpoint_read(self, path: str) -> None:
+        _check(self.lib.asph_checkpoint_read(self._ctx, str(path).encode()))
+
     def sync(self) -> None:
         _check(self.lib.asph_sync(self._ctx))
 
@@ -226,3 +260,120 @@ class Asph:
         _check(self.lib.asph_column_diag(self._ctx, _fptr(out)))
         return {"cloud_pct": float(out[0]), "ql_max": float(out[1]), "w_max": float(out[2]),
                 "precip_mm": float(out[3])}
+
+
+class Snapshot:
+    """Device memory holding one full state of a context."""
+
+    def __init__(self, sim: Asph):
+        self.lib = sim.lib
+        self._h = C.c_void_p()
+        _check(self.lib.asph_snapshot_create(sim._ctx, C.byref(self._h)))
+
+    def close(self) -> None:
+        if self._h:
+            self.lib.asph_snapshot_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Ensemble:
+    """Many independent simulations stepped together: one CUDA graph launch
+    per ensemble step forks into every member's step."""
+
+    def __init__(self, members: list, stream: int | None = None):
+        self.lib = library()
+        self.params = [p.copy() for p in members]
+        arr = (AsphParams * len(members))(*self.params)
+        self._h = C.c_void_p()
+        _check(self.lib.asph_ens_create(arr, len(members), C.c_void_p(stream or 0), C.byref(self._h)))
+        self._members = {}
+
+    def __len__(self) -> int:
+        return len(self.params)
+
+    @property
+    def n_particles(self) -> int:
+        return sum(int(p.n_particles) for p in self.params)
+
+    def close(self) -> None:
+        for m in self._members.values():
+            m._ctx = C.c_void_p()
+        self._members.clear()
+        if self._h:
+            self.lib.asph_ens_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init(self) -> None:
+        _check(self.lib.asph_ens_init(self._h))
+
+    def step(self, nsteps: int = 1) -> None:
+        _check(self.lib.asph_ens_step(self._h, int(nsteps)))
+
+    def step_async(self, nsteps: int = 1) -> None:
+        _check(self.lib.asph_ens_step_async(self._h, int(nsteps)))
+
+    def sync(self) -> None:
+        _check(self.lib.asph_ens_sync(self._h))
+
+    def member(self, k: int) -> Asph:
+        """The k-th member as an Asph view (state, audit, dump, options);
+        the ensemble owns it."""
+        ctx = C.c_void_p()
+        _check(self.lib.asph_ens_member(self._h, int(k), C.byref(ctx)))
+        m = self._members.get(k)
+        if m is None:
+            m = Asph(self.params[k], _borrowed=self)
+            self._members[k] = m
+        m._ctx = ctx
+        return m
+
+    def tune(self, trial_steps: int = 5, sort_choices=()) -> list:
+        """Per member (shape, sort cadence) picked by timing; the state is kept."""
+        n = len(self.params)
+        chosen = (C.c_int * (2 * n))()
+        sc = (C.c_int * max(1, len(sort_choices)))(*sort_choices)
+        _check(self.lib.asph_ens_tune(self._h, int(trial_steps), sc, len(sort_choices), chosen))
+        return [(chosen[2 * k], chosen[2 * k + 1]) for k in range(n)]
+
+
+def ensemble_members(count: int = 64, seed: int = 7, lo: int = 16384, hi: int = 524288,
+                     theta_sigma: float = 0.1, dt: float = 0.5) -> list:
+    """Members of uneven size: particle counts log-uniform in [lo, hi]
+    (seeded), each the 65,536-particle small-box atmosphere (h 200 x 200 x 50 m,
+    lattice spacing 312.5 x 312.5 x 78.125 m, +2 K bubble of 1 km radius at
+    1 km height) on an (n, n, 2n) lattice, n = round((N/2)^(1/3)), in a box
+    scaled with n so that the particle spacing and particles per cell stay
+    those of the small box; initial theta noise sigma [K]; member k seeds its
+    noise with k."""
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(np.log(lo), np.log(hi), count))
+    out = []
+    for k, nm in enumerate(counts):
+        n = int(round((nm / 2.0) ** (1.0 / 3.0)))
+        p = preset("small65k")
+        lx, lz = n * 312.5, 2 * n * 78.125
+        p.nx = p.ny = int(lx // 200.0)
+        p.nz = int(lz // 50.0)
+        p.dx = p.dy = lx / p.nx
+        p.dz = lz / p.nz
+        p.lat_nx = p.lat_ny = n
+        p.lat_nz = 2 * n
+        p.n_particles = 2 * n ** 3
+        p.bubble_x[0] = p.bubble_y[0] = lx / 2
+        p.noise = theta_sigma
+        p.seed = k
+        p.dt_request = dt
+        out.append(p)
+    return out

@@ -31,6 +31,7 @@ MAX_BUBBLES = 8
 NPHASES = 6
 OPT_PAIR_PATH = 1
 OPT_PAIR_SHAPE = 2
+OPT_SORT_EVERY = 3
 NOALLOC_MAX_KEYS = 524288
 NBR_CAP = 64
 PHASES = ("table_clear", "sort", "gather_kick_drift", "density_eos", "momentum_integrate", "step")
@@ -133,6 +134,21 @@ SIGNATURES = {
     "asph_column_diag": (C.c_int, [_P, _FP]),
     "asph_sort_keys_noalloc": (C.c_int, [_P, _P, _P, C.c_int, C.c_int, _P]),
     "asph_get_neighbours": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "asph_snapshot_create": (C.c_int, [_P, C.POINTER(_P)]),
+    "asph_snapshot_save": (C.c_int, [_P, _P]),
+    "asph_snapshot_restore": (C.c_int, [_P, _P]),
+    "asph_snapshot_destroy": (C.c_int, [_P]),
+    "asph_checkpoint_write": (C.c_int, [_P, C.c_char_p]),
+    "asph_checkpoint_read": (C.c_int, [_P, C.c_char_p]),
+    "asph_ens_create": (C.c_int, [C.POINTER(AsphParams), C.c_int, _P, C.POINTER(_P)]),
+    "asph_ens_destroy": (C.c_int, [_P]),
+    "asph_ens_size": (C.c_int, [_P]),
+    "asph_ens_member": (C.c_int, [_P, C.c_int, C.POINTER(_P)]),
+    "asph_ens_init": (C.c_int, [_P]),
+    "asph_ens_step": (C.c_int, [_P, C.c_int]),
+    "asph_ens_step_async": (C.c_int, [_P, C.c_int]),
+    "asph_ens_sync": (C.c_int, [_P]),
+    "asph_ens_tune": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int)]),
 }
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

@@ -3,6 +3,7 @@
 // the reference host loop, and the CUDA-graph step.
 #include <cuda_runtime.h>
 #include <stdarg.h>
+#include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -10,32 +11,13 @@
 #include <string>
 #include <vector>
 #include <sys/stat.h>
-#include "asph_internal.cuh"
-#include "../../include/asph.h"
+#include "asph_ctx.cuh"
 
 using namespace asph;
 
 namespace {
 
 thread_local std::string g_err;
-
-int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
-int fail(int code, const char* fmt, ...) {
-    char buf[512];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof(buf), fmt, ap);
-    va_end(ap);
-    g_err = buf;
-    return code;
-}
-
-#define CKR(x)                                                                                  \
-    do {                                                                                        \
-        cudaError_t e_ = (x);                                                                   \
-        if (e_ != cudaSuccess)                                                                  \
-            return fail(ASPH_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_)); \
-    } while (0)
 
 int ceil_log2(int n) {   // asph_h100.cu:865
     int b = 1;
@@ -45,52 +27,17 @@ int ceil_log2(int n) {   // asph_h100.cu:865
 
 }  // namespace
 
+int asph::fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
 int asph::set_error(int code, const char* msg) { return fail(code, "%s", msg); }
-
-struct GraphKey {
-    int pc, vc, qc, rc;
-};
-
-struct asph_ctx {
-    AsphParams prm;
-    Phys P;
-    Bufs B;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    bool initialised = false;
-    bool lists_valid = false;   // neighbour lists match the current positions
-    // graphs keyed by the ping-pong state at the start of the step
-    cudaGraphExec_t gexec[16] = {};
-    // staging for host <-> device SoA copies (16 floats per particle)
-    float* stage = nullptr;
-    // audit
-    double* audit_part = nullptr;
-    double* audit_out = nullptr;
-    int audit_blocks = 152 * 4;
-    // dumps
-    float* coarse = nullptr;
-    float4* coldiag = nullptr;
-    int cx = 0, cy = 0, cz = 0;
-    uint8_t* flags = nullptr;
-    std::vector<void*> allocs;
-
-    template <class T>
-    cudaError_t alloc(T** p, size_t bytes) {
-        void* q = nullptr;
-        cudaError_t e = cudaMalloc(&q, bytes < 256 ? 256 : bytes);
-        if (e == cudaSuccess) {
-            allocs.push_back(q);
-            *p = (T*)q;
-        }
-        return e;
-    }
-    ~asph_ctx() {
-        for (auto& g : gexec)
-            if (g) cudaGraphExecDestroy(g);
-        for (void* q : allocs) cudaFree(q);
-        if (own_stream && stream) cudaStreamDestroy(stream);
-    }
-};
 
 // ---------------------------------------------------------------------------
 // parameters
@@ -332,7 +279,7 @@ static int build_sounding(asph_ctx* c) {
     return ASPH_OK;
 }
 
-static int reset_control(asph_ctx* c) {
+int asph::reset_control(asph_ctx* c) {
     DevCtl h;
     memset(&h, 0, sizeof(h));
     h.simt = 0.0;
@@ -341,8 +288,10 @@ static int reset_control(asph_ctx* c) {
     h.sort_dt = 0.5f;
     h.dt_required = h.dt;
     h.do_sort = 1;
-    h.epoch = 0;
-    CKR(cudaMemcpyAsync(c->B.ctl, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+    // The radix look-back epoch is left as it is: status words written by
+    // earlier sorts of this context carry epochs up to the current one, so
+    // the epoch must only ever grow (it starts at 0 from asph_create).
+    CKR(cudaMemcpyAsync(c->B.ctl, &h, offsetof(DevCtl, epoch), cudaMemcpyHostToDevice, c->stream));
     return ASPH_OK;
 }
 
@@ -392,6 +341,7 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     B.skeys = B.kbuf[(B.npasses - 1) & 1];
     B.perm = B.vbuf[(B.npasses - 1) & 1];
     B.pc = B.vc = B.qc = B.rc = 0;
+    B.shape = -1;
     cudaStream_t s = c->stream;
     e = cudaMemsetAsync(B.status, 0, (size_t)B.npasses * B.ntiles * 256 * 8, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.range, 0, C * 8, s);
@@ -405,6 +355,7 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     if (e == cudaSuccess) e = cudaMemsetAsync(B.perm, 0, N * 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.skeys, 0, N * 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.nbr_cnt, 0xff, N * 4, s);   // -1: no list yet
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.ctl, 0, sizeof(DevCtl), s);
     if (e != cudaSuccess) {
         delete c;
         return fail(ASPH_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
@@ -427,7 +378,7 @@ extern "C" int asph_destroy(asph_ctx* c) {
 }
 
 // Collect the stream status and the device error word.
-static int sync_status(asph_ctx* c) {
+int asph::sync_status(asph_ctx* c) {
     CKR(cudaStreamSynchronize(c->stream));
     CKR(cudaGetLastError());
     int words[2];
@@ -443,10 +394,18 @@ extern "C" int asph_set_option(asph_ctx* c, int option, int value) {
     if (option == ASPH_OPT_PAIR_PATH) {
         if (value < 0 || value > 1) return fail(ASPH_ERR_ARG, "pair path must be 0 (auto) or 1 (global)");
         c->B.force_global = value;
+    } else if (option == ASPH_OPT_PAIR_SHAPE) {
+        if (value != -1 && !pair_shape_fits(c->P, value))
+            return fail(ASPH_ERR_ARG, "brick shape %d does not suit this grid and density", value);
+        c->B.shape = value;
+    } else if (option == ASPH_OPT_SORT_EVERY) {
+        if (value < 0) return fail(ASPH_ERR_ARG, "sort cadence must be >= 0");
+        c->P.sort_every = value;
+        c->prm.sort_every = value;
     } else {
         return fail(ASPH_ERR_ARG, "unknown option %d", option);
     }
-    for (auto& g : c->gexec)   // captured graphs hold the old kernels
+    for (auto& g : c->gexec)   // captured graphs hold the old kernels and parameters
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     return ASPH_OK;
 }
@@ -458,7 +417,11 @@ extern "C" int asph_get_option(asph_ctx* c, int option, int* value) {
         return ASPH_OK;
     }
     if (option == ASPH_OPT_PAIR_SHAPE) {
-        *value = c->B.force_global ? -1 : pair_shape(c->P);
+        *value = pair_shape(c->P, c->B);
+        return ASPH_OK;
+    }
+    if (option == ASPH_OPT_SORT_EVERY) {
+        *value = c->P.sort_every;
         return ASPH_OK;
     }
     return fail(ASPH_ERR_ARG, "unknown option %d", option);
@@ -472,7 +435,7 @@ extern "C" int asph_sync(asph_ctx* c) {
 // ---------------------------------------------------------------------------
 // granular blocks of the reference step
 // ---------------------------------------------------------------------------
-static bool reads_rain(const Phys& P) { return P.accretion || P.rain_evap; }
+bool asph::reads_rain(const Phys& P) { return P.accretion || P.rain_evap; }
 
 static void do_sort_build(asph_ctx* c, int force) {
     launch_sort_prep(c->P, c->B, force, 0, c->stream);
@@ -574,7 +537,7 @@ extern "C" int asph_set_state(asph_ctx* c, const AsphHostState* s) {
     return sync_status(c);
 }
 
-static void apply_pending_clamp(asph_ctx* c) { launch_clamp(c->P, c->B, c->stream); }
+void asph::apply_pending_clamp(asph_ctx* c) { launch_clamp(c->P, c->B, c->stream); }
 
 extern "C" int asph_get_state(asph_ctx* c, AsphHostState* s) {
     if (!c || !s) return fail(ASPH_ERR_ARG, "NULL argument");
@@ -755,7 +718,7 @@ extern "C" int asph_cfl(asph_ctx* c) {
 }
 
 // One full step: sort (gated on the device) -> G -> D -> M(+rain,+CFL).
-static void enqueue_step(asph_ctx* c) {
+void asph::enqueue_step(asph_ctx* c) {
     const Phys& P = c->P;
     launch_sort_prep(P, c->B, 0, reads_rain(P) ? 1 : 0, c->stream);
     launch_sort(P, c->B, 0, c->stream);
@@ -806,7 +769,7 @@ extern "C" int asph_step_profiled(asph_ctx* c, int nsteps, float* phase_ms) {
     return sync_status(c);
 }
 
-static int graph_slot(const Bufs& B) { return B.pc | (B.vc << 1) | (B.qc << 2) | (B.rc << 3); }
+int asph::graph_slot(const Bufs& B) { return B.pc | (B.vc << 1) | (B.qc << 2) | (B.rc << 3); }
 
 extern "C" int asph_step_async(asph_ctx* c, int nsteps) {
     if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");

@@ -1,0 +1,73 @@
+// asph_ctx.cuh — the context behind the opaque asph_ctx handle, shared by
+// the C-ABI translation units (asph_capi.cu, asph_ensemble.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <vector>
+#include "asph_internal.cuh"
+#include "../../include/asph.h"
+
+using namespace asph;
+
+struct asph_ctx {
+    AsphParams prm;
+    Phys P;
+    Bufs B;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bool initialised = false;
+    bool lists_valid = false;   // neighbour lists match the current positions
+    // graphs keyed by the ping-pong state at the start of the step
+    cudaGraphExec_t gexec[16] = {};
+    // staging for host <-> device SoA copies (16 floats per particle)
+    float* stage = nullptr;
+    // audit
+    double* audit_part = nullptr;
+    double* audit_out = nullptr;
+    int audit_blocks = 152 * 4;
+    // dumps
+    float* coarse = nullptr;
+    float4* coldiag = nullptr;
+    int cx = 0, cy = 0, cz = 0;
+    uint8_t* flags = nullptr;
+    std::vector<void*> allocs;
+
+    template <class T>
+    cudaError_t alloc(T** p, size_t bytes) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, bytes < 256 ? 256 : bytes);
+        if (e == cudaSuccess) {
+            allocs.push_back(q);
+            *p = (T*)q;
+        }
+        return e;
+    }
+    ~asph_ctx() {
+        for (auto& g : gexec)
+            if (g) cudaGraphExecDestroy(g);
+        for (void* q : allocs) cudaFree(q);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace asph {
+// Record a failure for asph_last_error(); returns `code`.
+int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+// Wait for the context's stream and turn the device error word / CFL abort
+// flag into a status.
+int sync_status(asph_ctx* c);
+// Enqueue one full step (sort, gather/kick/drift/flux, density, momentum)
+// on the context's stream and advance the ping-pong indices.
+void enqueue_step(asph_ctx* c);
+// Graph key of the ping-pong state at the start of a step.
+int graph_slot(const Bufs& B);
+void apply_pending_clamp(asph_ctx* c);
+bool reads_rain(const Phys& P);
+int reset_control(asph_ctx* c);
+}  // namespace asph
+
+#define CKR(x)                                                                                  \
+    do {                                                                                        \
+        cudaError_t e_ = (x);                                                                   \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail(ASPH_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_)); \
+    } while (0)

@@ -58,6 +58,7 @@ struct Bufs {
     int ntiles, npasses;
     int pc, vc, qc, rc; // current index of pos/vel/thq/rain ping-pong pairs
     int force_global;   // 1: pair passes take the per-target global path
+    int shape;          // brick shape index of the density pass, -1: automatic
 };
 
 // Mode bits of the gather/integrate pass.
@@ -87,7 +88,11 @@ void launch_gather(const Phys& P, const Bufs& B, int mode, cudaStream_t s);
 void launch_density(const Phys& P, const Bufs& B, cudaStream_t s);
 void launch_momentum(const Phys& P, const Bufs& B, int mode, int use_lists, cudaStream_t s);
 void launch_rain(const Phys& P, const Bufs& B, cudaStream_t s);
-int pair_shape(const Phys& P);
+// Brick shape index the density pass uses (-1: per-target global path),
+// the number of shapes, and whether shape k suits the grid and density.
+int pair_shape(const Phys& P, const Bufs& B);
+int pair_shape_count();
+bool pair_shape_fits(const Phys& P, int k);
 void launch_cfl(const Phys& P, const Bufs& B, cudaStream_t s);
 void launch_clamp(const Phys& P, const Bufs& B, cudaStream_t s);
 void launch_audit(const Phys& P, const Bufs& B, double* partial, int nblk, double* out, cudaStream_t s);

@@ -499,14 +499,21 @@ int region_cells(const Shape& s) { return (s.bx + 2 * HALO) * (s.by + 2 * HALO) 
 
 // Largest brick whose region fits the grid without wrapping onto itself
 // and whose expected staged count (with a margin) fits the cap.
+bool fits(const Phys& P, int k) {
+    const Shape& s = SHAPES[k];
+    if (P.nx < s.bx + 2 * HALO || P.ny < s.by + 2 * HALO) return false;
+    return region_cells(s) * ((double)P.N / (double)P.ncell) * STAGE_MARGIN <= MAX_STAGE;
+}
+
 int pick_shape(const Phys& P) {
-    const double ppc = (double)P.N / (double)P.ncell;
-    for (int k = 0; k < 4; ++k) {
-        const Shape& s = SHAPES[k];
-        if (P.nx < s.bx + 2 * HALO || P.ny < s.by + 2 * HALO) continue;
-        if (region_cells(s) * ppc * STAGE_MARGIN <= MAX_STAGE) return k;
-    }
+    for (int k = 0; k < 4; ++k)
+        if (fits(P, k)) return k;
     return -1;
+}
+
+int shape_in_use(const Phys& P, const Bufs& B) {
+    if (B.force_global) return -1;
+    return B.shape >= 0 ? B.shape : pick_shape(P);
 }
 
 struct Launch {
@@ -546,7 +553,9 @@ inline int blocks_for(int n, int tpb) { return n <= 0 ? 1 : (n + tpb - 1) / tpb;
 
 }  // namespace
 
-int pair_shape(const Phys& P) { return pick_shape(P); }
+int pair_shape(const Phys& P, const Bufs& B) { return shape_in_use(P, B); }
+int pair_shape_count() { return (int)(sizeof(SHAPES) / sizeof(SHAPES[0])); }
+bool pair_shape_fits(const Phys& P, int k) { return k >= 0 && k < pair_shape_count() && fits(P, k); }
 
 void launch_density(const Phys& P, const Bufs& B, cudaStream_t s) {
     DArgs A;
@@ -561,7 +570,7 @@ void launch_density(const Phys& P, const Bufs& B, cudaStream_t s) {
     A.nbr = B.nbr;
     A.nbr_cnt = B.nbr_cnt;
     A.ctl = B.ctl;
-    switch (B.force_global ? -1 : pick_shape(P)) {
+    switch (shape_in_use(P, B)) {
         case 0: launch_d<8, 8, 8>(P, A, s); break;
         case 1: launch_d<8, 8, 4>(P, A, s); break;
         case 2: launch_d<8, 4, 4>(P, A, s); break;
