@@ -288,6 +288,35 @@ int asph_ens_step_async(asph_ens* ens, int nsteps);
 int asph_ens_sync(asph_ens* ens);
 int asph_ens_tune(asph_ens* ens, int trial_steps, const int* sort_choices, int n_sort_choices, int* chosen);
 
+/* ---- adjoint window -----------------------------------------------------------
+ * No counterpart in the reference.  Gradients of a loss L of the final cloud
+ * water (and theta) after nsteps steps with respect to the initial theta of
+ * every particle and the viscosity coefficients alpha, beta.  The window
+ * step is the full step with the sort moved after the kick/drift/flux, so
+ * the neighbour lists hold exactly the pairs with q < 2; the sort
+ * (permutation), the lists and dt are held fixed in the adjoint.  The
+ * forward saves a device snapshot every `every` steps; the backward
+ * recomputes each segment from its snapshot, recording the per-step values
+ * the reverse needs, and runs the hand-written reverse kernels.
+ *   asph_adj_create    sizes the checkpoints and the segment tape for ctx
+ *   asph_adj_forward   runs the window from ctx's current state (its order
+ *                      is the order of dL_dtheta0) and leaves ctx at the end
+ *   asph_adj_backward  dL_dqc, dL_dtheta (N each), dL_dxyz (3 x N: x, y, z),
+ *                      any of them NULL: dL/d(final field) in the final
+ *                      state's order; writes
+ *                      dL_dtheta0[N] and dL_dalpha_beta[2] (may be NULL);
+ *                      ctx is left at the end of the window
+ * ASPH_ERR_STATE: a CFL trip or a neighbour-list overflow inside the window. */
+typedef struct asph_adj asph_adj;
+int asph_adj_create(asph_ctx* ctx, int nsteps, int every, asph_adj** out);
+int asph_adj_forward(asph_adj* adj);
+int asph_adj_backward(asph_adj* adj, const float* dL_dqc, const float* dL_dtheta, const float* dL_dxyz,
+                      float* dL_dtheta0, double* dL_dalpha_beta);
+int asph_adj_destroy(asph_adj* adj);
+/* Viscosity coefficients alpha (asph_h100.cu:84) and beta of the running
+ * context (the adjoint's parameters). */
+int asph_set_viscosity(asph_ctx* ctx, float alpha, float beta);
+
 /* ---- stable key sort without allocation -----------------------------------
  * No counterpart in the reference.  For callers that must not call
  * cudaMalloc/cudaFree (a latency-critical loop where cudaFree would

@@ -1,6 +1,8 @@
 """Build recipe for the oracle (test infrastructure only).
 
 * liboracle.so  — the FP64 C restatement (asph_oracle.c), gcc + OpenMP.
+* libadjhost.so — the FP64 host reference of the adjoint window
+  (adjoint_host.cpp): forward loss and reverse-mode gradient, g++.
 * _ref/asph_ref.cubin — the reference's device code compiled UNMODIFIED
   from the reference checkout with its own documented flags
   (asph_h100.cu:23-25: -O3 -use_fast_math -std=c++17), retargeted to
@@ -21,6 +23,7 @@ BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 REFERENCE_SRC = os.environ.get("ASPH_REFERENCE_SRC", "/root/reference/asph_h100.cu")
 LIBORACLE = os.path.join(BUILD, "liboracle.so")
+LIBADJHOST = os.path.join(BUILD, "libadjhost.so")
 CUBIN = os.path.join(REF_OUT, "asph_ref.cubin")
 REFGPU = os.path.join(BUILD, "refgpu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -54,6 +57,15 @@ def build_oracle(force: bool = False) -> str:
         _run(["gcc", "-O2", "-std=c11", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
               "-o", LIBORACLE, src, "-lm"])
     return LIBORACLE
+
+
+def build_adjoint_host(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "adjoint_host.cpp")
+    hdr = os.path.join(os.path.dirname(HERE), "include", "asph.h")
+    if force or _stale(LIBADJHOST, [src, hdr]):
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-o", LIBADJHOST, src])
+    return LIBADJHOST
 
 
 def build_ref_cubin(force: bool = False) -> str:
@@ -109,6 +121,7 @@ def build_refgpu(force: bool = False) -> str:
 
 def build_all(force: bool = False) -> None:
     build_oracle(force)
+    build_adjoint_host(force)
     build_ref_cubin(force)
     build_ref_cubin_bubble2m(force)
     build_refgpu(force)

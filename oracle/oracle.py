@@ -252,3 +252,55 @@ def run(p: AsphParams, state: dict, nsteps: int, rain_grid=None, precip=None, ct
     c = np.array(ctl if ctl is not None else [0.0, derived(p)["dt_cap"], 1e9, 0.5, 0, 0, 1, 0, 0], np.float64)
     st = lib().or_run(C.byref(p), int(nsteps), arr, _pd(rg), _pd(pr), _pd(c))
     return dict(zip(RUN_FIELDS, f)), rg, pr, c, st
+
+
+# ---- adjoint window (FP64 host reference; adjoint_host.cpp) -----------------
+ADJ_FIELDS = ("x", "y", "z", "u", "v", "w", "th", "qv", "qc", "rho", "ax", "ay", "az")
+_adj = None
+
+
+def adj_lib() -> C.CDLL:
+    global _adj
+    if _adj is None:
+        from . import build_oracle
+        _adj = C.CDLL(build_oracle.build_adjoint_host())
+        P = C.POINTER(AsphParams)
+        _adj.adj_host_loss.argtypes = [P, _D, _D, C.c_double, C.c_double, C.c_int, _D, _D, C.c_int, _D, _D]
+        _adj.adj_host_loss.restype = C.c_int
+        _adj.adj_host_grad.argtypes = [P, _D, _D, C.c_double, C.c_double, C.c_int, _D, _D, C.c_int, _D, _D, _D]
+        _adj.adj_host_grad.restype = C.c_long
+    return _adj
+
+
+def _adj_args(p, state, rain, alpha_beta, gauss):
+    st = np.ascontiguousarray(np.stack([_d(state[k]) for k in ADJ_FIELDS]))
+    rg = np.ascontiguousarray(_d(rain))
+    ab = np.ascontiguousarray(_d(alpha_beta))
+    g = np.ascontiguousarray(_d(gauss).reshape(-1, 6))
+    return st, rg, ab, g
+
+
+def adj_loss(p: AsphParams, state: dict, rain, simt: float, dt: float, nsteps: int, alpha_beta, gauss,
+             final: bool = False):
+    """FP64 window forward: loss (1/N) sum (qc - T(x))^2 after nsteps (and the final state)."""
+    st, rg, ab, g = _adj_args(p, state, rain, alpha_beta, gauss)
+    L = np.zeros(1)
+    fin = np.zeros_like(st) if final else None
+    _chk(adj_lib().adj_host_loss(C.byref(p), _pd(st), _pd(rg), float(simt), float(dt), int(nsteps), _pd(ab),
+                                 _pd(g), g.shape[0], _pd(L), _pd(fin) if final else None))
+    if final:
+        return float(L[0]), dict(zip(ADJ_FIELDS, fin))
+    return float(L[0])
+
+
+def adj_grad(p: AsphParams, state: dict, rain, simt: float, dt: float, nsteps: int, alpha_beta, gauss):
+    """FP64 host adjoint (reverse-mode over the FP64 window): (L, dL/dtheta0[N], dL/dalpha, dL/dbeta)."""
+    st, rg, ab, g = _adj_args(p, state, rain, alpha_beta, gauss)
+    L = np.zeros(1)
+    dth = np.zeros(p.n_particles)
+    dab = np.zeros(2)
+    n = adj_lib().adj_host_grad(C.byref(p), _pd(st), _pd(rg), float(simt), float(dt), int(nsteps), _pd(ab), _pd(g),
+                                g.shape[0], _pd(L), _pd(dth), _pd(dab))
+    if n <= 0:
+        raise RuntimeError("adj_host_grad failed")
+    return float(L[0]), dth, float(dab[0]), float(dab[1])

@@ -213,6 +213,11 @@ class Asph:
         """Brick shape of the density pass (0..3), -1 for automatic."""
         _check(self.lib.asph_set_option(self._ctx, abi.OPT_PAIR_SHAPE, int(shape)))
 
+    def set_viscosity(self, alpha: float, beta: float) -> None:
+        """Artificial-viscosity coefficients alpha and beta of the running context."""
+        _check(self.lib.asph_set_viscosity(self._ctx, float(alpha), float(beta)))
+        self.params.alpha_av, self.params.beta_av = float(alpha), float(beta)
+
     def sort_every(self) -> int:
         v = C.c_int()
         _check(self.lib.asph_get_option(self._ctx, abi.OPT_SORT_EVERY, C.byref(v)))

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 CU_SOURCES = ["asph_sort.cu", "asph_kernels.cu", "asph_pairs.cu", "asph_capi.cu", "asph_noalloc.cu",
-              "asph_ensemble.cu"]
+              "asph_ensemble.cu", "asph_adjoint.cu"]
 
 
 def nvcc() -> str:

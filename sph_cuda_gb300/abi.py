@@ -149,6 +149,11 @@ SIGNATURES = {
     "asph_ens_step_async": (C.c_int, [_P, C.c_int]),
     "asph_ens_sync": (C.c_int, [_P]),
     "asph_ens_tune": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int)]),
+    "asph_adj_create": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(_P)]),
+    "asph_adj_forward": (C.c_int, [_P]),
+    "asph_adj_backward": (C.c_int, [_P, _FP, _FP, _FP, _FP, C.POINTER(C.c_double)]),
+    "asph_adj_destroy": (C.c_int, [_P]),
+    "asph_set_viscosity": (C.c_int, [_P, C.c_float, C.c_float]),
 }
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

@@ -50,6 +50,7 @@ def _built():
     from oracle import build_oracle
     _build.build_library()
     build_oracle.build_oracle()
+    build_oracle.build_adjoint_host()
     yield
 
 
