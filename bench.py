@@ -389,6 +389,57 @@ def run_ensemble(args):
     return 0
 
 
+def run_adjoint(args):
+    """Adjoint window on the 262,144-particle small-box workload: K plain
+    steps against one window of K steps (forward with checkpoints every 10
+    steps, backward with recompute) of the final cloud-water misfit."""
+    import torch
+    import sph_cuda_gb300 as sph
+    from sph_cuda_gb300.adjoint import AdjointWindow, misfit, seeded_gaussians
+
+    torch.cuda.set_device(0)
+    p = sph.preset("adjoint262k")
+    sim = sph.Asph(p)
+    sim.init()
+    start = sim.snapshot()
+    K = args.steps
+    sim.step(max(args.warmup, 1))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.step(K)
+    t_plain = (time.perf_counter() - t0) / K
+    sim.restore(start)
+    sim.sync()
+    win = AdjointWindow(sim, K, 10)
+    gauss = seeded_gaussians(p.nx * p.dx, p.ny * p.dy, p.nz * p.dz, n=4, seed=0)
+    fin = win.forward()                      # warm: allocations, first launches
+    L, dqc, dxyz = misfit(fin, gauss)
+    win.backward(dL_dqc=dqc, dL_dxyz=dxyz)
+    t0 = time.perf_counter()
+    fin = win.forward()
+    t_fwd = time.perf_counter() - t0
+    L, dqc, dxyz = misfit(fin, gauss)
+    t0 = time.perf_counter()
+    dth, da, db = win.backward(dL_dqc=dqc, dL_dxyz=dxyz)
+    t_bwd = time.perf_counter() - t0
+    ratio = (t_fwd + t_bwd) / K / t_plain
+    line = {
+        "metric": "adjoint step time / forward step time (262,144 particles)", "value": ratio, "unit": "x",
+        "higher_is_better": False, "n_gpus": 1, "steps": K, "warmup": args.warmup, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "small-box atmosphere, 64 x 64 x 64 lattice, 50 x 50 x 100 cells, "
+                               "checkpoints every 10 steps, misfit of final cloud water to 4 seeded Gaussians",
+                   "particles": int(p.n_particles)},
+        "plain_ms_per_step": t_plain * 1e3, "window_forward_ms_per_step": t_fwd * 1e3 / K,
+        "backward_ms_per_step": t_bwd * 1e3 / K,
+        "loss": L, "grad": {"max_abs_dtheta0": float(np.abs(dth).max()), "dalpha": da, "dbeta": db},
+    }
+    print(json.dumps(line))
+    win.close()
+    sim.close()
+    return 0
+
+
 def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -397,7 +448,7 @@ def parse_args(argv=None):
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=0, help="0: about 12 s of oracle steps")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="bubble2m", choices=["bubble2m", "bubble524k", "ensemble64"])
+    ap.add_argument("--workload", default="bubble2m", choices=["bubble2m", "bubble524k", "ensemble64", "adjoint262k"])
     ap.add_argument("--no-tune", action="store_true", help="ensemble64: skip the autotuner")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
@@ -410,6 +461,8 @@ def main():
         return run_reference(args)
     if args.workload == "ensemble64":
         return run_ensemble(args)
+    if args.workload == "adjoint262k":
+        return run_adjoint(args)
     return run_ours(args)
 
 

@@ -240,10 +240,44 @@ int asph_audit(asph_ctx* ctx, double out[6]);
 /* Coarse dump in the reference format (asph_h100.cu:1080-1120), file name
  * <outdir>/asph_t%06.0fs.bin; `path` (may be NULL) receives the name. */
 int asph_dump(asph_ctx* ctx, const char* outdir, char* path, int path_len);
+/* The same dump in two halves, so that the device-to-host copy and the file
+ * write overlap the next steps: asph_dump_begin queues the coarse fields,
+ * the column diagnostics and the control block into pinned host memory on
+ * the context's stream (and restarts the precipitation accumulator, like
+ * asph_column_diag); steps may be queued after it; asph_dump_finish waits
+ * for that copy only, writes the file of the state at begin and fills
+ * diag[4] (may be NULL) as asph_column_diag does.  One dump in flight per
+ * context. */
+int asph_dump_begin(asph_ctx* ctx);
+int asph_dump_finish(asph_ctx* ctx, const char* outdir, char* path, int path_len, float diag[4]);
 /* Column diagnostics of the dump line (asph_h100.cu:1095-1105): cloud
  * cover [%], max ql [kg/kg], max |w| [m/s], mean precipitation [mm];
  * resets the precipitation accumulator like the reference. */
 int asph_column_diag(asph_ctx* ctx, float out[4]);
+
+/* ---- source-term hook ---------------------------------------------------------
+ * The reference's header defers radiation and ice/mixed-phase physics to
+ * "NN, additive source terms" (asph_h100.cu:14-15) without an interface.
+ * With the hook on, every step adds per-particle tendencies of theta [K/s],
+ * qv and qc [1/s] in its theta update (asph_h100.cu:562-571): theta +=
+ * (dthdt + S_theta) dt, qv += S_qv dt, qc += S_qc dt, then the caps.  The
+ * tendencies belong to particles: they are given in the context's current
+ * order and follow their particles through every later sort, so a set of
+ * tendencies stays attached until it is replaced.
+ *   asph_source_enable      allocates (zeroed) / detaches the buffer
+ *   asph_source_set         host arrays, any may be NULL (zero)
+ *   asph_source_set_device  a device float4[N] array {S_theta, S_qv, S_qc, -}
+ *                           (e.g. a model's output tensor), copied on the
+ *                           context's stream
+ *   asph_state_device       copies the current pos {x,y,z,rho_old}, vel
+ *                           {u,v,w,-} and thq {theta,qv,qc,-} (float4[N]
+ *                           each, any may be NULL) into caller device
+ *                           buffers on the context's stream
+ * The adjoint window runs without the hook. */
+int asph_source_enable(asph_ctx* ctx, int on);
+int asph_source_set(asph_ctx* ctx, const float* dtheta, const float* dqv, const float* dqc);
+int asph_source_set_device(asph_ctx* ctx, const void* tendencies);
+int asph_state_device(asph_ctx* ctx, void* pos, void* vel, void* thq);
 
 /* ---- state snapshots and restart files -------------------------------------
  * No counterpart in the reference (it cannot restart; its dumps are coarse

@@ -226,6 +226,40 @@ class Asph:
     def set_sort_every(self, k: int) -> None:
         _check(self.lib.asph_set_option(self._ctx, abi.OPT_SORT_EVERY, int(k)))
 
+    # ---- source-term hook ---------------------------------------------------------
+    def enable_source(self, on: bool = True) -> None:
+        """Per-particle additive tendencies of theta, qv, qc applied in every
+        step's theta update (zero after enabling)."""
+        _check(self.lib.asph_source_enable(self._ctx, int(bool(on))))
+
+    def set_source(self, dtheta=None, dqv=None, dqc=None) -> None:
+        """Tendencies [K/s, 1/s, 1/s] in the current particle order."""
+        keep = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (dtheta, dqv, dqc)]
+        for a in keep:
+            if a is not None and a.shape != (self.N,):
+                raise ValueError("tendency arrays must have shape (%d,)" % self.N)
+        _check(self.lib.asph_source_set(self._ctx, *[None if a is None else _fptr(a) for a in keep]))
+
+    def set_source_device(self, tendencies) -> None:
+        """Tendencies from a CUDA tensor of shape (N, 4) float32 {S_theta, S_qv, S_qc, -}."""
+        if tuple(tendencies.shape) != (self.N, 4) or not tendencies.is_contiguous():
+            raise ValueError("need a contiguous (N, 4) tensor")
+        import torch
+        torch.cuda.synchronize()   # the tensor's producer may run on another stream
+        _check(self.lib.asph_source_set_device(self._ctx, C.c_void_p(tendencies.data_ptr())))
+        self.sync()
+
+    def state_device(self, pos=None, vel=None, thq=None) -> None:
+        """Copy the current state into CUDA tensors of shape (N, 4) float32
+        (pos: x, y, z, rho_old; vel: u, v, w, -; thq: theta, qv, qc, -)."""
+        ptrs = []
+        for t in (pos, vel, thq):
+            if t is not None and (tuple(t.shape) != (self.N, 4) or not t.is_contiguous()):
+                raise ValueError("need contiguous (N, 4) tensors")
+            ptrs.append(None if t is None else C.c_void_p(t.data_ptr()))
+        _check(self.lib.asph_state_device(self._ctx, *ptrs))
+        self.sync()   # the tensors are read on torch's streams
+
     # ---- snapshots and restart files --------------------------------------------
     def snapshot(self) -> "Snapshot":
         """A device-resident copy of the full state (see restore)."""
@@ -259,6 +293,19 @@ class Asph:
         os.makedirs(outdir, exist_ok=True)
         _check(self.lib.asph_dump(self._ctx, outdir.encode(), buf, 1024))
         return buf.value.decode()
+
+    def dump_begin(self) -> None:
+        """Queue a dump of the current state (asynchronous device-to-host copy)."""
+        _check(self.lib.asph_dump_begin(self._ctx))
+
+    def dump_finish(self, outdir: str):
+        """Write the dump queued by dump_begin; returns (path, column diagnostics)."""
+        buf = C.create_string_buffer(1024)
+        diag = np.zeros(4, np.float32)
+        os.makedirs(outdir, exist_ok=True)
+        _check(self.lib.asph_dump_finish(self._ctx, outdir.encode(), buf, 1024, _fptr(diag)))
+        return buf.value.decode(), {"cloud_pct": float(diag[0]), "ql_max": float(diag[1]),
+                                    "w_max": float(diag[2]), "precip_mm": float(diag[3])}
 
     def column_diag(self) -> dict:
         out = np.zeros(4, np.float32)

@@ -154,6 +154,12 @@ SIGNATURES = {
     "asph_adj_backward": (C.c_int, [_P, _FP, _FP, _FP, _FP, C.POINTER(C.c_double)]),
     "asph_adj_destroy": (C.c_int, [_P]),
     "asph_set_viscosity": (C.c_int, [_P, C.c_float, C.c_float]),
+    "asph_dump_begin": (C.c_int, [_P]),
+    "asph_dump_finish": (C.c_int, [_P, C.c_char_p, C.c_char_p, C.c_int, _FP]),
+    "asph_source_enable": (C.c_int, [_P, C.c_int]),
+    "asph_source_set": (C.c_int, [_P, _FP, _FP, _FP]),
+    "asph_source_set_device": (C.c_int, [_P, _P]),
+    "asph_state_device": (C.c_int, [_P, _P, _P, _P]),
 }
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

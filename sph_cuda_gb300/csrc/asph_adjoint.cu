@@ -672,6 +672,9 @@ int af_step(asph_adj* a, StepTape* t) {
     Bufs& B = c->B;
     cudaStream_t s = c->stream;
     const size_t N = (size_t)P.N, C = (size_t)P.ncell;
+    // the window runs without the source-term hook (its tendencies are not differentiated)
+    float4* const src = B.src;
+    B.src = nullptr;
 #define CP_(dst, src, bytes) CKR(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyDeviceToDevice, s))
     if (t) {
         CP_(t->pos0, B.pos[B.pc], N * 16); CP_(t->vel0, B.vel[B.vc], N * 16); CP_(t->thq0, B.thq[B.qc], N * 16);
@@ -699,6 +702,7 @@ int af_step(asph_adj* a, StepTape* t) {
     launch_momentum(P, B, M_INTEGRATE | M_RAIN | M_CFL, 1, s);
     B.nbr = nbr;
     B.nbr_cnt = nbr_cnt;
+    B.src = src;
     B.vc ^= 1; B.rc ^= 1;
     if (t) {
         CP_(t->acc, B.acc, N * 16); CP_(t->dthdt, B.dthdt, N * 4);

@@ -427,6 +427,58 @@ extern "C" int asph_get_option(asph_ctx* c, int option, int* value) {
     return fail(ASPH_ERR_ARG, "unknown option %d", option);
 }
 
+// ---------------------------------------------------------------------------
+// source-term hook
+// ---------------------------------------------------------------------------
+static void drop_graphs(asph_ctx* c) {
+    for (auto& g : c->gexec)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
+extern "C" int asph_source_enable(asph_ctx* c, int on) {
+    if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
+    const size_t N = (size_t)c->P.N;
+    if (on && !c->src_mem) {
+        CKR(c->alloc(&c->src_mem, N * 32));
+        CKR(cudaMemsetAsync(c->src_mem, 0, N * 32, c->stream));
+    }
+    c->B.src = on ? c->src_mem : nullptr;
+    c->B.src_tmp = on ? c->src_mem + N : nullptr;
+    drop_graphs(c);   // the captured steps hold the buffer pointers
+    return ASPH_OK;
+}
+
+extern "C" int asph_source_set(asph_ctx* c, const float* dth, const float* dqv, const float* dqc) {
+    if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
+    if (!c->B.src) return fail(ASPH_ERR_STATE, "source-term hook is off (asph_source_enable)");
+    const size_t N = (size_t)c->P.N;
+    std::vector<float4> h(N);
+    for (size_t i = 0; i < N; ++i)
+        h[i] = make_float4(dth ? dth[i] : 0.f, dqv ? dqv[i] : 0.f, dqc ? dqc[i] : 0.f, 0.f);
+    CKR(cudaMemcpyAsync(c->B.src, h.data(), N * 16, cudaMemcpyHostToDevice, c->stream));
+    CKR(cudaStreamSynchronize(c->stream));
+    return ASPH_OK;
+}
+
+extern "C" int asph_source_set_device(asph_ctx* c, const void* tendencies) {
+    if (!c || !tendencies) return fail(ASPH_ERR_ARG, "NULL argument");
+    if (!c->B.src) return fail(ASPH_ERR_STATE, "source-term hook is off (asph_source_enable)");
+    CKR(cudaMemcpyAsync(c->B.src, tendencies, (size_t)c->P.N * 16, cudaMemcpyDeviceToDevice, c->stream));
+    return ASPH_OK;
+}
+
+extern "C" int asph_state_device(asph_ctx* c, void* pos, void* vel, void* thq) {
+    if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
+    if (!c->initialised) return fail(ASPH_ERR_STATE, "no state yet (init/set_state)");
+    apply_pending_clamp(c);
+    const size_t n = (size_t)c->P.N * 16;
+    Bufs& B = c->B;
+    if (pos) CKR(cudaMemcpyAsync(pos, B.pos[B.pc], n, cudaMemcpyDeviceToDevice, c->stream));
+    if (vel) CKR(cudaMemcpyAsync(vel, B.vel[B.vc], n, cudaMemcpyDeviceToDevice, c->stream));
+    if (thq) CKR(cudaMemcpyAsync(thq, B.thq[B.qc], n, cudaMemcpyDeviceToDevice, c->stream));
+    return ASPH_OK;
+}
+
 extern "C" int asph_sync(asph_ctx* c) {
     if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
     return sync_status(c);
@@ -442,6 +494,9 @@ static void do_sort_build(asph_ctx* c, int force) {
     launch_sort(c->P, c->B, force, c->stream);
     launch_gather(c->P, c->B, G_SORTED | (force ? G_FORCE : 0), c->stream);
     c->B.pc ^= 1; c->B.vc ^= 1; c->B.qc ^= 1;
+    // source-term tendencies follow their particles (a step keeps them in its momentum pass)
+    if (c->B.src)
+        cudaMemcpyAsync(c->B.src, c->B.src_tmp, (size_t)c->P.N * 16, cudaMemcpyDeviceToDevice, c->stream);
 }
 
 extern "C" int asph_init(asph_ctx* c) {
@@ -865,6 +920,82 @@ extern "C" int asph_dump(asph_ctx* c, const char* outdir, char* path, int path_l
     hh.nfields = 6; hh.t_sim = (float)ctl.simt; hh.dt = ctl.dt;
     hh.lx = c->P.lx; hh.ly = c->P.ly; hh.lz = c->P.lz;
     const bool ok = fwrite(&hh, sizeof(hh), 1, f) == 1 && fwrite(h.data(), 4, n, f) == n;
+    fclose(f);
+    if (!ok) return fail(ASPH_ERR_IO, "short write to %s", fn);
+    if (path && path_len > 0) snprintf(path, (size_t)path_len, "%s", fn);
+    return ASPH_OK;
+}
+
+// Asynchronous dump: the coarse fields, the column diagnostics, the surface
+// precipitation and the control block are copied into pinned host memory on
+// the context's stream; steps queued afterwards run while the copy completes
+// and the file is written.
+extern "C" int asph_dump_begin(asph_ctx* c) {
+    if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
+    if (c->dump_pending) return fail(ASPH_ERR_STATE, "a dump is already in flight (asph_dump_finish)");
+    int st = ensure_dump(c);
+    if (st) return st;
+    const size_t n = (size_t)c->cx * c->cy * c->cz * 6, ncol = (size_t)c->P.nxy;
+    if (!c->h_dump) {
+        CKR(cudaMallocHost(&c->h_dump, n * 4 + ncol * 20 + sizeof(DevCtl)));
+        CKR(cudaEventCreateWithFlags(&c->dump_ev, cudaEventDisableTiming));
+    }
+    apply_pending_clamp(c);
+    const AsphParams& p = c->prm;
+    launch_coarse(c->P, c->B, c->coarse, p.dump_sx, p.dump_sy, p.dump_sz, c->cx, c->cy, c->cz, c->coldiag, c->stream);
+    CKR(cudaGetLastError());
+    char* h = (char*)c->h_dump;
+    CKR(cudaMemcpyAsync(h, c->coarse, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    CKR(cudaMemcpyAsync(h + n * 4, c->coldiag, ncol * 16, cudaMemcpyDeviceToHost, c->stream));
+    CKR(cudaMemcpyAsync(h + n * 4 + ncol * 16, c->B.precip, ncol * 4, cudaMemcpyDeviceToHost, c->stream));
+    CKR(cudaMemcpyAsync(h + n * 4 + ncol * 20, c->B.ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, c->stream));
+    // the precipitation accumulator restarts at every dump (asph_h100.cu:1105)
+    CKR(cudaMemsetAsync(c->B.precip, 0, ncol * 4, c->stream));
+    CKR(cudaEventRecord(c->dump_ev, c->stream));
+    c->dump_pending = true;
+    return ASPH_OK;
+}
+
+extern "C" int asph_dump_finish(asph_ctx* c, const char* outdir, char* path, int path_len, float diag[4]) {
+    if (!c || !outdir) return fail(ASPH_ERR_ARG, "NULL argument");
+    if (!c->dump_pending) return fail(ASPH_ERR_STATE, "no dump in flight (asph_dump_begin)");
+    c->dump_pending = false;
+    CKR(cudaEventSynchronize(c->dump_ev));
+    const AsphParams& p = c->prm;
+    const size_t n = (size_t)c->cx * c->cy * c->cz * 6, ncol = (size_t)c->P.nxy;
+    const char* h = (const char*)c->h_dump;
+    const float* coarse = (const float*)h;
+    const float4* cd = (const float4*)(h + n * 4);
+    const float* pr = (const float*)(h + n * 4 + ncol * 16);
+    DevCtl ctl;
+    memcpy(&ctl, h + n * 4 + ncol * 20, sizeof ctl);
+    if (diag) {
+        int ncloud = 0;
+        float qlmax = 0.f, wmax = 0.f, psum = 0.f;
+        for (size_t k = 0; k < ncol; ++k) {   // asph_h100.cu:1095-1102
+            if (cd[k].z > 1e-4f) ++ncloud;
+            qlmax = fmaxf(qlmax, cd[k].z);
+            wmax = fmaxf(wmax, cd[k].w);
+            psum += pr[k];
+        }
+        diag[0] = ncol ? 100.f * (float)ncloud / ncol : 0.f;
+        diag[1] = qlmax;
+        diag[2] = wmax;
+        diag[3] = ncol ? psum / ncol : 0.f;
+    }
+    mkdir(outdir, 0775);
+    char fn[1024];
+    snprintf(fn, sizeof(fn), "%s/asph_t%06.0fs.bin", outdir, ctl.simt);   // asph_h100.cu:1107
+    FILE* f = fopen(fn, "wb");
+    if (!f) return fail(ASPH_ERR_IO, "cannot open %s", fn);
+    DumpHeader hh{};
+    hh.magic = 0x41535048u; hh.version = 3;
+    hh.nx = p.nx; hh.ny = p.ny; hh.nz = p.nz;
+    hh.cx = c->cx; hh.cy = c->cy; hh.cz = c->cz;
+    hh.sx = p.dump_sx; hh.sy = p.dump_sy; hh.sz = p.dump_sz;
+    hh.nfields = 6; hh.t_sim = (float)ctl.simt; hh.dt = ctl.dt;
+    hh.lx = c->P.lx; hh.ly = c->P.ly; hh.lz = c->P.lz;
+    const bool ok = fwrite(&hh, sizeof(hh), 1, f) == 1 && fwrite(coarse, 4, n, f) == n;
     fclose(f);
     if (!ok) return fail(ASPH_ERR_IO, "short write to %s", fn);
     if (path && path_len > 0) snprintf(path, (size_t)path_len, "%s", fn);

@@ -218,6 +218,17 @@ int main(int argc, char** argv) {
                                                     "momentum+integrate+rain+cfl", "step"};
     AsphControl ctl;
     asph_get_control(run.ctx, &ctl);
+    struct {
+        bool on = false;
+        long long step = 0;
+        AsphControl ctl;
+    } pending;
+    auto print_dump = [&](long long at_step, const AsphControl& c, const float* cd) {
+        std::printf("%-8lld +%-8.0fs %-8.1f %-9.4f CFL %.2f | cloud %5.2f%% ql_max %.3f g/kg | w_max %5.2f m/s | "
+                    "precip %.3f mm\n",
+                    at_step, c.simt, now_s() - wall0, c.dt, c.dt_required > 0 ? c.dt / c.dt_required : 0.f, cd[0],
+                    cd[1] * 1e3f, cd[2], cd[3]);
+    };
 
     std::printf("\n%-8s %-9s %-8s %-9s %s\n", "step", "sim time", "wall s", "dt s", "CFL / cloud / precip");
     while (ctl.simt < sim_end && (cli.max_steps < 0 || step < cli.max_steps)) {
@@ -233,28 +244,39 @@ int main(int argc, char** argv) {
         if (n > to_prof) n = to_prof;
         if (cli.max_steps >= 0 && n > cli.max_steps - step) n = cli.max_steps - step;
         if (n > 1 << 20) n = 1 << 20;
-        if ((step + n) % 50 == 0) {
-            if (n > 1 && (st = asph_step(run.ctx, (int)(n - 1)))) break;
+        const bool profiled = (step + n) % 50 == 0;
+        if (profiled) {
+            if (n > 1 && (st = asph_step_async(run.ctx, (int)(n - 1)))) break;
+        } else if ((st = asph_step_async(run.ctx, (int)n))) {
+            break;
+        }
+        // a dump begun after the previous chunk is written while this chunk runs
+        if (pending.on) {
+            char fn[1024];
+            float cd[4];
+            pending.on = false;
+            if ((st = asph_dump_finish(run.ctx, cli.outdir.c_str(), fn, sizeof fn, cd))) break;
+            ++dumps;
+            print_dump(pending.step, pending.ctl, cd);
+        }
+        if ((st = asph_sync(run.ctx))) break;
+        if (profiled) {
             float ph[ASPH_NPHASES];
             if ((st = asph_step_profiled(run.ctx, 1, ph))) break;
             for (int k = 0; k < ASPH_NPHASES; ++k) phase_acc[k] += ph[k];
-        } else if ((st = asph_step(run.ctx, (int)n))) {
-            break;
         }
         step += n;
         asph_get_control(run.ctx, &ctl);
 
         if (ctl.simt >= next_dump) {
-            char fn[1024];
-            if ((st = asph_dump(run.ctx, cli.outdir.c_str(), fn, sizeof fn))) break;
-            ++dumps;
-            float cd[4];
-            if ((st = asph_column_diag(run.ctx, cd))) break;
-            std::printf("%-8lld +%-8.0fs %-8.1f %-9.4f CFL %.2f | cloud %5.2f%% ql_max %.3f g/kg | w_max %5.2f m/s | "
-                        "precip %.3f mm\n",
-                        step, ctl.simt, now_s() - wall0, ctl.dt, ctl.dt_required > 0 ? ctl.dt / ctl.dt_required : 0.f,
-                        cd[0], cd[1] * 1e3f, cd[2], cd[3]);
             if (cli.validate) {
+                // the audit reads the state of the dump: dump synchronously
+                char fn[1024];
+                float cd[4];
+                if ((st = asph_dump(run.ctx, cli.outdir.c_str(), fn, sizeof fn))) break;
+                ++dumps;
+                if ((st = asph_column_diag(run.ctx, cd))) break;
+                print_dump(step, ctl, cd);
                 if ((st = asph_audit(run.ctx, tot))) break;
                 const double e0 = tot0[0] + tot0[1] + tot0[2], e1 = tot[0] + tot[1] + tot[2];
                 std::printf("  AUDIT  KE %.4e  PE %.4e  IE %.4e  E_tot %.4e  water %.4e  pz %.4e\n", tot[0], tot[1],
@@ -262,6 +284,11 @@ int main(int argc, char** argv) {
                 std::printf("  DRIFT  dKE %.2e  dE %.2e (%.3f%%/h)  dwater %.2e\n", tot[0] - tot0[0], e1 - e0,
                             100.0 * (e1 - e0) / std::fmax(1.0, std::fabs(e0)) * 3600.0 / std::fmax(1.0, ctl.simt),
                             tot[3] - tot0[3]);
+            } else {
+                if ((st = asph_dump_begin(run.ctx))) break;
+                pending.on = true;
+                pending.step = step;
+                pending.ctl = ctl;
             }
             next_dump += cli.dump_every;
         }
@@ -277,6 +304,16 @@ int main(int argc, char** argv) {
             std::printf("\n");
             wall_report = wall;
             sim_report = ctl.simt;
+        }
+    }
+    if (pending.on && st == ASPH_OK) {
+        char fn[1024];
+        float cd[4];
+        pending.on = false;
+        st = asph_dump_finish(run.ctx, cli.outdir.c_str(), fn, sizeof fn, cd);
+        if (st == ASPH_OK) {
+            ++dumps;
+            print_dump(pending.step, pending.ctl, cd);
         }
     }
     asph_get_control(run.ctx, &ctl);

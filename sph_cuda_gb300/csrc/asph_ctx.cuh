@@ -29,6 +29,12 @@ struct asph_ctx {
     float4* coldiag = nullptr;
     int cx = 0, cy = 0, cz = 0;
     uint8_t* flags = nullptr;
+    // source-term hook: tendencies and their per-step copy (2 x float4[N])
+    float4* src_mem = nullptr;
+    // asynchronous dump: pinned host copy and its completion event
+    void* h_dump = nullptr;
+    cudaEvent_t dump_ev = nullptr;
+    bool dump_pending = false;
     std::vector<void*> allocs;
 
     template <class T>
@@ -42,6 +48,8 @@ struct asph_ctx {
         return e;
     }
     ~asph_ctx() {
+        if (h_dump) cudaFreeHost(h_dump);
+        if (dump_ev) cudaEventDestroy(dump_ev);
         for (auto& g : gexec)
             if (g) cudaGraphExecDestroy(g);
         for (void* q : allocs) cudaFree(q);

@@ -267,6 +267,8 @@ struct MOut {
     float4* acc;
     float* dthdt;
     float4* vel_out;
+    const float4* src_cur;   // source-term tendencies in this step's order (NULL: hook off)
+    float4* src_keep;        // where they are kept for the next step
 };
 __device__ __forceinline__ float3 momentum_epilogue(const Phys& P, const MOut& O, int i, const MTarget& T, MSum s,
                                                     bool integrate, float dt) {
@@ -284,7 +286,16 @@ __device__ __forceinline__ float3 momentum_epilogue(const Phys& P, const MOut& O
     O.dthdt[i] = dthc;
     float3 m = make_float3(0.f, 0.f, 0.f);
     if (integrate) {
-        ti.x = fminf(fmaxf(ti.x + dthc * dt, 100.0f), P.theta_cap);
+        if (O.src_cur) {
+            // source-term hook: additive tendencies before the theta update
+            const float4 sv = O.src_cur[i];
+            O.src_keep[i] = sv;
+            ti.x = fminf(fmaxf(ti.x + (dthc + sv.x) * dt, 100.0f), P.theta_cap);
+            ti.y = fminf(fmaxf(ti.y + sv.y * dt, 0.0f), P.qv_cap);
+            ti.z = fmaxf(ti.z + sv.z * dt, 0.0f);
+        } else {
+            ti.x = fminf(fmaxf(ti.x + dthc * dt, 100.0f), P.theta_cap);
+        }
         O.thq[i] = ti;
         const float hdt = 0.5f * dt;
         float4 vn = make_float4(T.u + s.ax * hdt, T.v + s.ay * hdt, T.w + s.az * hdt, 0.f);

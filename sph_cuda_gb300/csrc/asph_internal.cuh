@@ -59,6 +59,8 @@ struct Bufs {
     int pc, vc, qc, rc; // current index of pos/vel/thq/rain ping-pong pairs
     int force_global;   // 1: pair passes take the per-target global path
     int shape;          // brick shape index of the density pass, -1: automatic
+    float4* src;        // source-term hook: per-particle tendencies (theta, qv, qc), NULL when off
+    float4* src_tmp;    // the tendencies in the order of the current step (written by the gather)
 };
 
 // Mode bits of the gather/integrate pass.

@@ -88,6 +88,8 @@ struct GArgs {
     int2* range;
     uint8_t* surf;
     uint32_t* kin;
+    const float4* src;   // source-term tendencies (NULL: hook off) ...
+    float4* src_tmp;     // ... follow their particles through the gather
     DevCtl* ctl;
 };
 
@@ -172,6 +174,7 @@ __global__ __launch_bounds__(TPB) void k_gather(const __grid_constant__ Phys P, 
         A.pos_dst[i] = make_float4(p.x, p.y, p.z, rho);
         A.vel_dst[i] = v;
         A.thq_dst[i] = t;
+        if (A.src) A.src_tmp[i] = A.src[s];
         A.kin[i] = key_of(P, p.x, p.y, p.z);
     }
 }
@@ -335,6 +338,7 @@ void launch_gather(const Phys& P, const Bufs& B, int mode, cudaStream_t s) {
     A.pos_dst = B.pos[1 - B.pc]; A.vel_dst = B.vel[1 - B.vc]; A.thq_dst = B.thq[1 - B.qc];
     A.rp = B.rp; A.acc = B.acc; A.perm = B.perm; A.skeys = B.skeys; A.range = B.range;
     A.surf = B.surf; A.kin = B.kin; A.ctl = B.ctl;
+    A.src = B.src; A.src_tmp = B.src_tmp;
     k_gather<<<blocks_for(P.N), TPB, 0, s>>>(P, A, mode);
 }
 

@@ -592,6 +592,8 @@ void launch_momentum(const Phys& P, const Bufs& B, int mode, int use_lists, cuda
     A.out.acc = B.acc;
     A.out.dthdt = B.dthdt;
     A.out.vel_out = B.vel[1 - B.vc];
+    A.out.src_cur = B.src ? B.src_tmp : nullptr;
+    A.out.src_keep = B.src;
     A.rain_in = B.rain[B.rc];
     A.rain_delta = (P.accretion || P.rain_evap) ? B.rain_delta : nullptr;
     A.rain_out = B.rain[1 - B.rc];
