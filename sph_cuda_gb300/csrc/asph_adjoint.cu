@@ -341,6 +341,7 @@ __global__ __launch_bounds__(ATPB) void k_adj_mom_pairs(const Phys P, StepTape T
             const int j = T.lst[(size_t)q * P.N + i];
             const float4 xj = T.pos1[j], vj = T.vel1[j], sFj = A.sF[j], sVj = A.sV[j];
             const float2 rj = T.rp[j];
+            if (r2_cells(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z) >= 4.f) continue;   // the pass's own test
             const float rx = xi.x - xj.x, ry = xi.y - xj.y, rz = xi.z - xj.z;
             const float dxt = rx * P.inv_dx, dyt = ry * P.inv_dy, dzt = rz * P.inv_dz;
             const float r2t = dxt * dxt + dyt * dyt + dzt * dzt;
@@ -511,8 +512,7 @@ __global__ void k_adj_dens_a(const Phys P, StepTape T, AdjBufs A) {
     for (int q = 0; q < cnt; ++q) {
         const int j = T.lst[(size_t)q * P.N + i];
         const float4 xj = T.pos1[j];
-        const float dxt = (xi.x - xj.x) * P.inv_dx, dyt = (xi.y - xj.y) * P.inv_dy, dzt = (xi.z - xj.z) * P.inv_dz;
-        const float r2t = dxt * dxt + dyt * dyt + dzt * dzt;
+        const float r2t = r2_cells(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z);
         if (r2t >= 4.f || r2t < 1e-12f) continue;
         const float W = w3(sqrtf(r2t));
         S1 += W;
@@ -552,6 +552,7 @@ __global__ __launch_bounds__(ATPB) void k_adj_dens_b(const Phys P, StepTape T, A
         const int j = T.lst[(size_t)q * P.N + i];
         const float4 xj = T.pos1[j];
         const float2 lSj = A.lS[j];
+        if (r2_cells(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z) >= 4.f) continue;   // the pass's own test
         const float rx = xi.x - xj.x, ry = xi.y - xj.y, rz = xi.z - xj.z;
         const float dxt = rx * P.inv_dx, dyt = ry * P.inv_dy, dzt = rz * P.inv_dz;
         const float r2t = dxt * dxt + dyt * dyt + dzt * dzt;

@@ -33,6 +33,23 @@ __device__ __forceinline__ FF snd_eval(const float4* __restrict__ tab, int nnode
     return r;
 }
 
+// Pair distances in cell units.  Every acceptance test (brick and global
+// paths, the momentum fallback, the adjoint) uses these two functions, so
+// all of them accept exactly the same pairs: each coordinate is scaled to
+// cell units with one rounded product, the differences are exact float
+// subtractions, and r^2 is formed with explicit fused multiply-adds.
+__device__ __forceinline__ float3 to_cells(const Phys& P, float x, float y, float z) {
+    return make_float3(__fmul_rn(x, P.inv_dx), __fmul_rn(y, P.inv_dy), __fmul_rn(z, P.inv_dz));
+}
+__device__ __forceinline__ float r2_scaled(float ax, float ay, float az, float bx, float by, float bz) {
+    const float dx = ax - bx, dy = ay - by, dz = az - bz;
+    return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+}
+__device__ __forceinline__ float r2_cells(const Phys& P, float xi, float yi, float zi, float xj, float yj, float zj) {
+    const float3 a = to_cells(P, xi, yi, zi), b = to_cells(P, xj, yj, zj);
+    return r2_scaled(a.x, a.y, a.z, b.x, b.y, b.z);
+}
+
 // Stop the run from inside a kernel: record the reason (first one wins)
 // and make every later kernel of the step and of later steps do nothing.
 __device__ __forceinline__ void stop_run(DevCtl* ctl, int code) {

@@ -166,10 +166,6 @@ __device__ __forceinline__ void for_window_smem(const int* s_off, int lx, int ly
     }
 }
 
-__device__ __forceinline__ float r2_cells(const Phys& P, float xi, float yi, float zi, float xj, float yj, float zj) {
-    const float dx = (xi - xj) * P.inv_dx, dy = (yi - yj) * P.inv_dy, dz = (zi - zj) * P.inv_dz;
-    return dx * dx + dy * dy + dz * dz;
-}
 
 // Neighbour-list writer of one target (slot-major, coalesced over targets).
 struct NbrOut {
@@ -230,7 +226,7 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
     using G = BrickGeom<BX, BY, BZ>;
     extern __shared__ __align__(16) unsigned char smem[];
     const int T = blockDim.x;
-    float4* sp = reinterpret_cast<float4*>(smem);                       // x, y, z, rho_old
+    float4* sp = reinterpret_cast<float4*>(smem);                       // x, y, z in cell units, rho_old
     int* s_gidx = reinterpret_cast<int*>(sp + C.cap);                    // global index of a staged slot
     int* s_off = s_gidx + C.cap;                                         // R + 1
     int* s_start = s_off + (G::R + 1);                                   // R
@@ -282,7 +278,9 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
         for (int l = l0; l < l1; ++l) {
             const int o = s_off[l], c = s_off[l + 1] - o, st = s_start[l];
             for (int k = 0; k < c; ++k) {
-                sp[o + k] = A.pos[st + k];
+                const float4 q = A.pos[st + k];
+                const float3 u = to_cells(P, q.x, q.y, q.z);   // compared in cell units
+                sp[o + k] = make_float4(u.x, u.y, u.z, q.w);
                 s_gidx[o + k] = st + k;
             }
         }
@@ -296,12 +294,14 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
         const int i = base + lane;
         const bool active = i < te;
         float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+        float3 ci = make_float3(0.f, 0.f, 0.f);   // pi in cell units
         FF rr{0.f, 0.f};
         DSum s{0.f, 0.f, 0.f};
         int lx = 0, ly = 0, zlo = 0, zhi = -1;
         bool fast = false;
         if (active) {
             pi = A.pos[i];
+            ci = to_cells(P, pi.x, pi.y, pi.z);
             rr = snd_eval(P.snd_rho, P.snd_n, pi.z);
             fast = staged && local_window<BX, BY, BZ>(P, bxi, byi, bzi, pi.x, pi.y, pi.z, lx, ly, zlo, zhi);
         }
@@ -315,7 +315,7 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
             if (q < n) {                                                              \
                 const int kq = s_list[q * T + threadIdx.x];                           \
                 const float4 pj = sp[kq];                                             \
-                const float r2 = r2_cells(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z);     \
+                const float r2 = r2_scaled(ci.x, ci.y, ci.z, pj.x, pj.y, pj.z);       \
                 dsum_add(s, r2, pj.w, rr);                                            \
                 if (r2 >= 1e-12f) L.push(s_gidx[kq]);                                 \
             }                                                                         \
@@ -333,7 +333,7 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
                 if (!done) {
                     if (k < kend) {
                         const float4 pj = sp[k];
-                        if (r2_cells(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z) < 4.0f)
+                        if (r2_scaled(ci.x, ci.y, ci.z, pj.x, pj.y, pj.z) < 4.0f)
                             s_list[(n++) * T + threadIdx.x] = (unsigned short)k;
                         ++k;
                     } else if (++jy > ly + STENCIL && (jy = ly - STENCIL, ++jz > zhi)) {

@@ -117,7 +117,7 @@ __global__ __launch_bounds__(SORT_TPB) void k_hist(const uint32_t* __restrict__ 
     }
 }
 
-__global__ __launch_bounds__(SORT_TPB) void k_radix_pass(
+__global__ __launch_bounds__(SORT_TPB, 4) void k_radix_pass(
     const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
     uint32_t* __restrict__ vout, uint64_t* __restrict__ status, int N, int ntiles, int pass,
     DevCtl* __restrict__ ctl, int force) {
