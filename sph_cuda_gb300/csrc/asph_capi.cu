@@ -559,7 +559,55 @@ __global__ void k_unpack(Phys P, float* __restrict__ st, const float4* pos, cons
     st[10 * N + i] = a.x; st[11 * N + i] = a.y; st[12 * N + i] = a.z;
     st[13 * N + i] = r.y; st[14 * N + i] = dthdt[i];
 }
+// The same packing straight from / into pinned host arrays: the kernel
+// reads and writes host memory over the host link, so the fields need no
+// staging copy (one pass each way instead of a copy plus a pass).
+struct HostFields {
+    float* f[15];   // device-usable addresses of the caller's pinned arrays, NULL = absent
+};
+__global__ void k_pack_host(Phys P, HostFields H, float4* pos, float4* vel, float4* thq, float2* rp, float4* acc,
+                            float* dthdt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    auto f = [&](int k) { return H.f[k] ? H.f[k][i] : 0.f; };
+    const float rho = f(9);
+    pos[i] = make_float4(f(0), f(1), f(2), rho);
+    vel[i] = make_float4(f(3), f(4), f(5), 0.f);
+    thq[i] = make_float4(f(6), f(7), f(8), 0.f);
+    rp[i] = make_float2(rho, f(13));
+    acc[i] = make_float4(f(10), f(11), f(12), 0.f);
+    dthdt[i] = f(14);
+}
+__global__ void k_unpack_host(Phys P, HostFields H, const float4* pos, const float4* vel, const float4* thq,
+                              const float2* rp, const float4* acc, const float* dthdt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const float4 p = pos[i], v = vel[i], t = thq[i], a = acc[i];
+    const float2 r = rp[i];
+    const float val[15] = {p.x, p.y, p.z, v.x, v.y, v.z, t.x, t.y, t.z, r.x, a.x, a.y, a.z, r.y, dthdt[i]};
+#pragma unroll
+    for (int k = 0; k < 15; ++k)
+        if (H.f[k]) H.f[k][i] = val[k];
+}
 }  // namespace asph
+
+// Device-usable addresses of the non-NULL fields when every one of them is
+// pinned (page-locked) host memory; false otherwise (pageable arrays take
+// the staged path).
+static bool pinned_fields(float* const f[15], HostFields* H) {
+    for (int k = 0; k < 15; ++k) {
+        H->f[k] = nullptr;
+        if (!f[k]) continue;
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, f[k]) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+        H->f[k] = (float*)a.devicePointer;
+    }
+    return true;
+}
 
 static float* const* state_fields(const AsphHostState* s, float* out[15]) {
     float* f[15] = {s->x, s->y, s->z, s->u, s->v, s->w, s->th, s->qv, s->qc, s->rho, s->ax, s->ay, s->az, s->prs, s->dthdt};
@@ -573,18 +621,24 @@ extern "C" int asph_set_state(asph_ctx* c, const AsphHostState* s) {
     state_fields(s, f);
     for (int k = 0; k < 10; ++k)
         if (!f[k]) return fail(ASPH_ERR_ARG, "set_state: field %d (x..rho) is required", k);
-    int st = ensure_stage(c);
-    if (st) return st;
-    const size_t N = (size_t)c->P.N;
-    unsigned mask = 0;
-    for (int k = 0; k < 15; ++k) {
-        if (!f[k]) continue;
-        mask |= 1u << k;
-        CKR(cudaMemcpyAsync(c->stage + k * N, f[k], N * 4, cudaMemcpyHostToDevice, c->stream));
-    }
     Bufs& B = c->B;
-    k_pack<<<(c->P.N + TPB - 1) / TPB, TPB, 0, c->stream>>>(c->P, c->stage, mask, B.pos[B.pc], B.vel[B.vc],
-                                                            B.thq[B.qc], B.rp, B.acc, B.dthdt);
+    HostFields H;
+    if (pinned_fields(f, &H)) {
+        k_pack_host<<<(c->P.N + TPB - 1) / TPB, TPB, 0, c->stream>>>(c->P, H, B.pos[B.pc], B.vel[B.vc], B.thq[B.qc],
+                                                                     B.rp, B.acc, B.dthdt);
+    } else {
+        int st = ensure_stage(c);
+        if (st) return st;
+        const size_t N = (size_t)c->P.N;
+        unsigned mask = 0;
+        for (int k = 0; k < 15; ++k) {
+            if (!f[k]) continue;
+            mask |= 1u << k;
+            CKR(cudaMemcpyAsync(c->stage + k * N, f[k], N * 4, cudaMemcpyHostToDevice, c->stream));
+        }
+        k_pack<<<(c->P.N + TPB - 1) / TPB, TPB, 0, c->stream>>>(c->P, c->stage, mask, B.pos[B.pc], B.vel[B.vc],
+                                                                B.thq[B.qc], B.rp, B.acc, B.dthdt);
+    }
     launch_keys(c->P, B, c->stream);
     CKR(cudaGetLastError());
     c->initialised = true;
@@ -596,15 +650,23 @@ void asph::apply_pending_clamp(asph_ctx* c) { launch_clamp(c->P, c->B, c->stream
 
 extern "C" int asph_get_state(asph_ctx* c, AsphHostState* s) {
     if (!c || !s) return fail(ASPH_ERR_ARG, "NULL argument");
-    int st = ensure_stage(c);
-    if (st) return st;
     apply_pending_clamp(c);
     Bufs& B = c->B;
+    float* f[15];
+    state_fields(s, f);
+    HostFields H;
+    if (pinned_fields(f, &H)) {
+        k_unpack_host<<<(c->P.N + TPB - 1) / TPB, TPB, 0, c->stream>>>(c->P, H, B.pos[B.pc], B.vel[B.vc],
+                                                                       B.thq[B.qc], B.rp, B.acc, B.dthdt);
+        CKR(cudaGetLastError());
+        CKR(cudaStreamSynchronize(c->stream));
+        return ASPH_OK;
+    }
+    int st = ensure_stage(c);
+    if (st) return st;
     k_unpack<<<(c->P.N + TPB - 1) / TPB, TPB, 0, c->stream>>>(c->P, c->stage, B.pos[B.pc], B.vel[B.vc], B.thq[B.qc],
                                                               B.rp, B.acc, B.dthdt);
     CKR(cudaGetLastError());
-    float* f[15];
-    state_fields(s, f);
     const size_t N = (size_t)c->P.N;
     for (int k = 0; k < 15; ++k)
         if (f[k]) CKR(cudaMemcpyAsync(f[k], c->stage + k * N, N * 4, cudaMemcpyDeviceToHost, c->stream));
