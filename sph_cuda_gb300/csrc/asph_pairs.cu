@@ -390,7 +390,7 @@ __device__ __noinline__ MSum momentum_target_global(const Phys& P, const MArgs& 
     return s;
 }
 
-__global__ __launch_bounds__(M_TPB) void k_momentum(const __grid_constant__ Phys P, const __grid_constant__ MArgs A,
+__global__ __launch_bounds__(M_TPB, 4) void k_momentum(const __grid_constant__ Phys P, const __grid_constant__ MArgs A,
                                                     int mode) {
     __shared__ float s_max[3][M_TPB / 32];
     __shared__ bool s_last;
