@@ -323,13 +323,13 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
         n = 0;                                                                        \
     } while (0)
         // flattened walk of the window rows in the staged region; the warp
-        // votes once per 4 steps, so queues drain at DLIST - 4
+        // votes once per 8 steps, so queues drain at DLIST - 8
         bool done = !fast;
         int jz = zlo, jy = ly - STENCIL, k = 0, kend = 0;
         if (!done) row_span(s_off, (jz * G::RY + jy) * G::RX + lx - STENCIL, k, kend);
         for (;;) {
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < 8; ++u) {
                 if (!done) {
                     if (k < kend) {
                         const float4 pj = sp[k];
@@ -343,7 +343,7 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
                     }
                 }
             }
-            if (__any_sync(0xffffffffu, n > DLIST - 4)) ASPH_DRAIN();
+            if (__any_sync(0xffffffffu, n > DLIST - 8)) ASPH_DRAIN();
             if (__all_sync(0xffffffffu, done)) break;
         }
         ASPH_DRAIN();
