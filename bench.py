@@ -267,6 +267,17 @@ def run_ours(args):
             traffic = json.load(open(tfile)).get(dom)
         except Exception:
             traffic = None
+    # the pair kernels are bound by instruction issue and load latency, not
+    # HBM: their pipe utilisation from the committed ncu capture goes beside
+    # the HBM fraction
+    companion = None
+    pfile = os.path.join(ROOT, "profiles", "pipes_bubble2m.txt")
+    if os.path.exists(pfile):
+        try:
+            d = json.load(open(pfile))
+            companion = dict(d.get(dom, {}), source=d.get("source"))
+        except Exception:
+            companion = None
 
     # end to end through the C ABI with pinned host buffers: per step the
     # persistent state goes host->device, one step runs, the state comes back
@@ -308,6 +319,7 @@ def run_ours(args):
                        "parallelism": "replicas x%d" % ws},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
+                         "companion": companion,
                          "step_achieved": algo["step"] / (ph_ms["step"] / 1e3) / 1e9,
                          "kernel_ms": ph_ms},
             "cpu_baseline": cpu,
