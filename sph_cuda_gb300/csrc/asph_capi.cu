@@ -332,6 +332,14 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     AL(B.ctl, sizeof(DevCtl));
     AL(B.nbr, (size_t)NBR_CAP * N * 4);
     AL(B.nbr_cnt, N * 4);
+    sort_inc_sizes(P.N, &B.inc_max, &B.inc_tiles, &B.inc_blocks);
+    AL(B.inc_u, N * 4);
+    for (int k = 0; k < 2; ++k) {
+        AL(B.inc_k[k], (size_t)B.inc_max * 4);
+        AL(B.inc_i[k], (size_t)B.inc_max * 4);
+    }
+    AL(B.inc_cnt, (size_t)B.inc_blocks * 4);
+    AL(B.inc_status, (size_t)B.npasses * B.inc_tiles * 256 * 8);
 #undef AL
     if (e != cudaSuccess) {
         delete c;
@@ -344,6 +352,7 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     B.shape = -1;
     cudaStream_t s = c->stream;
     e = cudaMemsetAsync(B.status, 0, (size_t)B.npasses * B.ntiles * 256 * 8, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.inc_status, 0, (size_t)B.npasses * B.inc_tiles * 256 * 8, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.range, 0, C * 8, s);
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaMemsetAsync(B.rain[k], 0, C * 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.rain_delta, 0, C * 4, s);

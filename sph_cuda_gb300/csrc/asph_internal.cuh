@@ -30,6 +30,12 @@ struct DevCtl {
     unsigned epoch;            // radix look-back epoch
     unsigned hist[MAX_PASSES][256];
     unsigned tile_ctr[MAX_PASSES];
+    // incremental sort (sort lane 1): keys that changed since the last sort
+    unsigned inc_m;            // how many changed this step
+    int inc_on;                // 1: this step sorts incrementally
+    unsigned iepoch;           // look-back epoch of the changed-key sort
+    unsigned ihist[MAX_PASSES][256];
+    unsigned itile_ctr[MAX_PASSES];
 };
 
 // Buffers of one context.  Particle buffers hold 16-byte field groups.
@@ -46,6 +52,14 @@ struct Bufs {
     uint32_t* skeys;    // sorted keys of the last sort (points into kbuf)
     uint32_t* perm;     // permutation of the last sort (points into vbuf)
     uint64_t* status;   // look-back words [pass][tile][digit]
+    // incremental sort: unchanged indices, changed keys/indices (ping-pong),
+    // per-block counts, the changed-key sort's look-back words
+    uint32_t* inc_u;
+    uint32_t* inc_k[2];
+    uint32_t* inc_i[2];
+    uint32_t* inc_cnt;
+    uint64_t* inc_status;
+    int inc_max, inc_tiles, inc_blocks;
     int2*   range;      // cell table, {start,end}, {0,0} when empty
     uint8_t* surf;      // 1 when the particle was in the lowest layer at the last sort
     float*  rain[2];    // Eulerian rain mass per cell [kg]
@@ -86,6 +100,8 @@ void launch_init(const Phys& P, const Bufs& B, const float* bub, int nbub, int i
 void launch_keys(const Phys& P, const Bufs& B, cudaStream_t s);
 void launch_sort_prep(const Phys& P, const Bufs& B, int force, int clear_delta, cudaStream_t s);
 void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s);
+// Sizes of the incremental sort's buffers for N particles.
+void sort_inc_sizes(int N, int* max_keys, int* tiles, int* blocks);
 void launch_gather(const Phys& P, const Bufs& B, int mode, cudaStream_t s);
 void launch_density(const Phys& P, const Bufs& B, cudaStream_t s);
 void launch_momentum(const Phys& P, const Bufs& B, int mode, int use_lists, cudaStream_t s);

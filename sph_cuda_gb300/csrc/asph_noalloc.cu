@@ -26,10 +26,11 @@
 namespace asph {
 
 // Kernels of asph_sort.cu, launched unchanged.
-__global__ void k_hist(const uint32_t* __restrict__ keys, int N, int npasses, DevCtl* __restrict__ ctl, int force);
+__global__ void k_hist(const uint32_t* __restrict__ keys, int N, int npasses, DevCtl* __restrict__ ctl, int force,
+                       int lane);
 __global__ void k_radix_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                              uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint64_t* __restrict__ status,
-                             int N, int ntiles, int pass, DevCtl* __restrict__ ctl, int force);
+                             int N, int ntiles, int pass, DevCtl* __restrict__ ctl, int force, int lane);
 
 namespace {
 
@@ -91,7 +92,7 @@ extern "C" int asph_sort_keys_noalloc(const uint32_t* keys, uint32_t* keys_sorte
     k_noalloc_prep<<<1, 256, 0, s>>>(ctl);
     int hb = (n + TPB * 8 - 1) / (TPB * 8);
     hb = hb > 152 * 8 ? 152 * 8 : hb;
-    k_hist<<<hb, SORT_TPB, 0, s>>>(keys, n, npasses, ctl, 1);
+    k_hist<<<hb, SORT_TPB, 0, s>>>(keys, n, npasses, ctl, 1, 0);
     const uint32_t* ki = keys;
     const uint32_t* vi = nullptr;
     for (int p = 0; p < npasses; ++p) {
@@ -99,7 +100,7 @@ extern "C" int asph_sort_keys_noalloc(const uint32_t* keys, uint32_t* keys_sorte
         const bool to_out = ((npasses - 1 - p) % 2) == 0;
         uint32_t* ko = to_out ? keys_sorted : sk;
         uint32_t* vo = to_out ? perm : sv;
-        k_radix_pass<<<ntiles, SORT_TPB, 0, s>>>(ki, vi, ko, vo, status, n, ntiles, p, ctl, 1);
+        k_radix_pass<<<ntiles, SORT_TPB, 0, s>>>(ki, vi, ko, vo, status, n, ntiles, p, ctl, 1, 0);
         ki = ko;
         vi = vo;
     }

@@ -33,6 +33,14 @@ __device__ __forceinline__ bool sort_runs(const DevCtl* ctl, int force) {
     return force || (ctl->do_sort && !ctl->aborted);
 }
 
+// Sort lane 0 is the full sort of all keys; lane 1 sorts the keys that
+// changed since the last sort (incremental path).  The step launches both;
+// the control block decides which one works.
+__device__ __forceinline__ bool lane_runs(const DevCtl* ctl, int force, int sort_lane) {
+    if (sort_lane == 0) return force || (ctl->do_sort && !ctl->aborted && !ctl->inc_on);
+    return !force && ctl->do_sort && !ctl->aborted && ctl->inc_on;
+}
+
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
     asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -101,8 +109,10 @@ __global__ void k_sort_prep(Phys P, int2* __restrict__ range, float* __restrict_
 
 // Digit histograms of every pass in one read of the keys.
 __global__ __launch_bounds__(SORT_TPB) void k_hist(const uint32_t* __restrict__ keys, int N, int npasses,
-                                                   DevCtl* __restrict__ ctl, int force) {
-    if (!sort_runs(ctl, force)) return;
+                                                   DevCtl* __restrict__ ctl, int force, int sort_lane) {
+    if (!lane_runs(ctl, force, sort_lane)) return;
+    if (sort_lane) N = min(N, (int)ctl->inc_m);
+    unsigned* ghist = sort_lane ? &ctl->ihist[0][0] : &ctl->hist[0][0];
     __shared__ uint32_t h[MAX_PASSES][256];
     for (int i = threadIdx.x; i < MAX_PASSES * 256; i += blockDim.x) (&h[0][0])[i] = 0u;
     __syncthreads();
@@ -113,15 +123,18 @@ __global__ __launch_bounds__(SORT_TPB) void k_hist(const uint32_t* __restrict__ 
     __syncthreads();
     for (int i = threadIdx.x; i < npasses * 256; i += blockDim.x) {
         uint32_t c = (&h[0][0])[i];
-        if (c) atomicAdd(&(&ctl->hist[0][0])[i], c);
+        if (c) atomicAdd(&ghist[i], c);
     }
 }
 
 __global__ __launch_bounds__(SORT_TPB, 4) void k_radix_pass(
     const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
     uint32_t* __restrict__ vout, uint64_t* __restrict__ status, int N, int ntiles, int pass,
-    DevCtl* __restrict__ ctl, int force) {
-    if (!sort_runs(ctl, force)) return;
+    DevCtl* __restrict__ ctl, int force, int sort_lane) {
+    if (!lane_runs(ctl, force, sort_lane)) return;
+    if (sort_lane) N = min(N, (int)ctl->inc_m);
+    unsigned* const tile_ctr = sort_lane ? ctl->itile_ctr : ctl->tile_ctr;
+    const unsigned* const ghist = sort_lane ? ctl->ihist[pass] : ctl->hist[pass];
     constexpr int NW = SORT_TPB / 32;
     __shared__ uint32_t s_whist[NW][256];
     __shared__ uint32_t s_keys[SORT_TILE];
@@ -132,13 +145,14 @@ __global__ __launch_bounds__(SORT_TPB, 4) void k_radix_pass(
     __shared__ uint32_t s_tile;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) s_tile = atomicAdd(&ctl->tile_ctr[pass], 1u);
+    if (tid == 0) s_tile = atomicAdd(&tile_ctr[pass], 1u);
     for (int i = tid; i < NW * 256; i += SORT_TPB) (&s_whist[0][0])[i] = 0u;
     __syncthreads();
     const int tile = (int)s_tile;
     const int shift = 8 * pass;
     const int base = tile * SORT_TILE;
-    const unsigned epoch = ctl->epoch;
+    if (base >= N && tile > 0) return;   // lane 1 launches for its largest count
+    const unsigned epoch = sort_lane ? ctl->iepoch : ctl->epoch;
 
     uint32_t k[SORT_ITEMS], v[SORT_ITEMS], r[SORT_ITEMS];
     uint32_t d[SORT_ITEMS];
@@ -207,7 +221,7 @@ __global__ __launch_bounds__(SORT_TPB, 4) void k_radix_pass(
     // Global start of each digit (scan of the histogram) and the tile-local
     // start of each digit (scan of the tile counts).
     uint32_t tot;
-    const uint32_t gstart = block_excl_scan(ctl->hist[pass][dg], s_scan, &tot);
+    const uint32_t gstart = block_excl_scan(ghist[dg], s_scan, &tot);
     const uint32_t texcl = block_excl_scan(tile_cnt, s_scan, &tot);
     s_texcl[dg] = texcl;
     s_gbase[dg] = gstart + excl;
@@ -223,7 +237,7 @@ __global__ __launch_bounds__(SORT_TPB, 4) void k_radix_pass(
         }
     }
     __syncthreads();
-    const int nvalid = min(SORT_TILE, N - base);
+    const int nvalid = max(0, min(SORT_TILE, N - base));
     for (int j = tid; j < nvalid; j += SORT_TPB) {
         const uint32_t key = s_keys[j];
         const uint32_t dd = (key >> shift) & 255u;
@@ -235,6 +249,183 @@ __global__ __launch_bounds__(SORT_TPB, 4) void k_radix_pass(
     }
 }
 
+// ---------------------------------------------------------------------------
+// Incremental sort.  The particles are in the order of the last sort, whose
+// sorted keys are B.skeys.  A particle whose key did not change keeps its
+// place in that sorted sequence, so the unchanged particles, in index order,
+// are already sorted by (key, index); only the changed ones need a sort.
+// Their stable sort merged with the unchanged sequence by (key, index) is
+// exactly the stable sort of all keys, bit for bit.  When more than a
+// fixed share changed (inc_max), the full sort runs instead.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int INC_TPB = 256;
+constexpr int INC_CHUNK = INC_TPB * 8;   // keys per compaction block
+constexpr int MERGE_ITEMS = 8;           // outputs per merge thread
+
+__device__ __forceinline__ bool inc_step_sorts(const DevCtl* ctl) { return ctl->do_sort && !ctl->aborted; }
+}  // namespace
+
+__global__ __launch_bounds__(INC_TPB) void k_inc_count(const uint32_t* __restrict__ kin,
+                                                       const uint32_t* __restrict__ sprev, int N,
+                                                       uint32_t* __restrict__ cnt, const DevCtl* __restrict__ ctl) {
+    if (!inc_step_sorts(ctl)) return;
+    __shared__ uint32_t s_red[INC_TPB / 32];
+    const int base = blockIdx.x * INC_CHUNK;
+    const int end = min(base + INC_CHUNK, N);
+    uint32_t c = 0;
+    for (int e = base + threadIdx.x; e < end; e += INC_TPB) c += kin[e] != sprev[e] ? 1u : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < INC_TPB / 32; ++w) t += s_red[w];
+        cnt[blockIdx.x] = t;
+    }
+}
+
+// One block: block counts -> exclusive offsets; decides the path.
+__global__ void k_inc_scan(uint32_t* __restrict__ cnt, int nblocks, int inc_max, DevCtl* __restrict__ ctl) {
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_carry;
+    if (!inc_step_sorts(ctl)) {
+        if (threadIdx.x == 0) ctl->inc_on = 0;
+        return;
+    }
+    if (threadIdx.x == 0) s_carry = 0u;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int b0 = 0; b0 < nblocks; b0 += blockDim.x) {
+        const int b = b0 + threadIdx.x;
+        const uint32_t v = b < nblocks ? cnt[b] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = lane < nw ? s_warp[lane] : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            if (lane < nw) s_warp[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t carry = s_carry;
+        const uint32_t off = carry + (warp ? s_warp[warp - 1] : 0u) + x - v;
+        if (b < nblocks) cnt[b] = off;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry = carry + s_warp[nw - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const uint32_t m = s_carry;
+        ctl->inc_m = m;
+        ctl->inc_on = m <= (uint32_t)inc_max ? 1 : 0;
+        ctl->iepoch += 1u;
+    }
+    for (int i = threadIdx.x; i < MAX_PASSES * 256; i += blockDim.x) (&ctl->ihist[0][0])[i] = 0u;
+    if (threadIdx.x < MAX_PASSES) ctl->itile_ctr[threadIdx.x] = 0u;
+}
+
+// Split into the unchanged indices (in order) and the changed keys/indices.
+__global__ __launch_bounds__(INC_TPB) void k_inc_split(const uint32_t* __restrict__ kin,
+                                                       const uint32_t* __restrict__ sprev, int N,
+                                                       const uint32_t* __restrict__ off, uint32_t* __restrict__ uidx,
+                                                       uint32_t* __restrict__ ck, uint32_t* __restrict__ ci,
+                                                       const DevCtl* __restrict__ ctl) {
+    if (!inc_step_sorts(ctl) || !ctl->inc_on) return;
+    __shared__ uint32_t s_warp[INC_TPB / 32];
+    const int base = blockIdx.x * INC_CHUNK;
+    uint32_t oc = off[blockIdx.x];          // changed before this block
+    uint32_t ou = (uint32_t)base - oc;      // unchanged before this block
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int r = 0; r < INC_CHUNK; r += INC_TPB) {
+        const int e = base + r + threadIdx.x;
+        const bool in = e < N;
+        const uint32_t k = in ? kin[e] : 0u;
+        const bool ch = in && k != sprev[e];
+        const unsigned m = __ballot_sync(0xffffffffu, ch);
+        if (lane == 0) s_warp[warp] = __popc(m);
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+        for (int w = 0; w < INC_TPB / 32; ++w) {
+            const uint32_t c = s_warp[w];
+            if (w < warp) before += c;
+            total += c;
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        const uint32_t rc = before + __popc(m & lt);                       // changed before e in this round
+        const uint32_t ru = (uint32_t)(warp * 32 + lane) - rc;             // unchanged before e in this round
+        if (ch) {
+            ck[oc + rc] = k;
+            ci[oc + rc] = (uint32_t)e;
+        } else if (in) {
+            uidx[ou + ru] = (uint32_t)e;
+        }
+        oc += total;
+        ou += (uint32_t)min(INC_TPB, max(0, N - (base + r))) - total;
+        __syncthreads();
+    }
+}
+
+// Merge of the unchanged sequence (uidx, keys kin[uidx]) and the sorted
+// changed sequence (ck, ci) by (key, index): merge path, MERGE_ITEMS outputs
+// per thread.
+__device__ __forceinline__ bool key_idx_less(uint32_t ka, uint32_t ia, uint32_t kb, uint32_t ib) {
+    return ka < kb || (ka == kb && ia < ib);
+}
+__global__ __launch_bounds__(INC_TPB) void k_inc_merge(const uint32_t* __restrict__ uidx,
+                                                       const uint32_t* __restrict__ kin,
+                                                       const uint32_t* __restrict__ ck,
+                                                       const uint32_t* __restrict__ ci, int N,
+                                                       uint32_t* __restrict__ skeys, uint32_t* __restrict__ perm,
+                                                       const DevCtl* __restrict__ ctl) {
+    if (!inc_step_sorts(ctl) || !ctl->inc_on) return;
+    const int m = (int)ctl->inc_m, nu = N - m;
+    const long long p0 = ((long long)blockIdx.x * INC_TPB + threadIdx.x) * MERGE_ITEMS;
+    if (p0 >= N) return;
+    int lo = (int)max(0LL, p0 - nu), hi = (int)min(p0, (long long)m);
+    while (lo < hi) {   // how many changed keys come first among the first p0 outputs
+        const int mid = (lo + hi) >> 1;
+        const uint32_t ua = uidx[p0 - 1 - mid];
+        if (key_idx_less(ck[mid], ci[mid], kin[ua], ua)) lo = mid + 1;
+        else hi = mid;
+    }
+    int b = lo, a = (int)p0 - lo;
+    for (int j = 0; j < MERGE_ITEMS && p0 + j < N; ++j) {
+        bool take_c = b < m;
+        uint32_t ua = 0, ku = 0;
+        if (a < nu) {
+            ua = uidx[a];
+            ku = kin[ua];
+            take_c = take_c && key_idx_less(ck[b], ci[b], ku, ua);
+        }
+        if (take_c) {
+            skeys[p0 + j] = ck[b];
+            perm[p0 + j] = ci[b];
+            ++b;
+        } else {
+            skeys[p0 + j] = ku;
+            perm[p0 + j] = ua;
+            ++a;
+        }
+    }
+}
+
+void sort_inc_sizes(int N, int* max_keys, int* tiles, int* blocks) {
+    *max_keys = N / 8 > 0 ? N / 8 : 1;   // above this share of changed keys the full sort runs
+    *tiles = (*max_keys + SORT_TILE - 1) / SORT_TILE;
+    *blocks = (N + INC_CHUNK - 1) / INC_CHUNK;
+}
+
 void launch_sort_prep(const Phys& P, const Bufs& B, int force, int clear_delta, cudaStream_t s) {
     int blocks = (P.ncell / 2 + TPB - 1) / TPB;
     blocks = blocks < 1 ? 1 : (blocks > 152 * 16 ? 152 * 16 : blocks);
@@ -243,14 +434,40 @@ void launch_sort_prep(const Phys& P, const Bufs& B, int force, int clear_delta, 
 
 void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s) {
     if (P.N <= 0) return;
+    const bool inc = !force && B.inc_u;
+    if (inc) {
+        // decide the path: count the changed keys (lane 1 runs when few changed)
+        k_inc_count<<<B.inc_blocks, INC_TPB, 0, s>>>(B.kin, B.skeys, P.N, B.inc_cnt, B.ctl);
+        k_inc_scan<<<1, 1024, 0, s>>>(B.inc_cnt, B.inc_blocks, B.inc_max, B.ctl);
+    }
     int hb = (P.N + TPB * 8 - 1) / (TPB * 8);
     hb = hb > 152 * 8 ? 152 * 8 : hb;
-    k_hist<<<hb, SORT_TPB, 0, s>>>(B.kin, P.N, B.npasses, B.ctl, force);
+    k_hist<<<hb, SORT_TPB, 0, s>>>(B.kin, P.N, B.npasses, B.ctl, force, 0);
     for (int p = 0; p < B.npasses; ++p) {
         const uint32_t* ki = p == 0 ? B.kin : B.kbuf[(p - 1) & 1];
         const uint32_t* vi = p == 0 ? nullptr : B.vbuf[(p - 1) & 1];
         k_radix_pass<<<B.ntiles, SORT_TPB, 0, s>>>(ki, vi, B.kbuf[p & 1], B.vbuf[p & 1], B.status, P.N,
-                                                   B.ntiles, p, B.ctl, force);
+                                                   B.ntiles, p, B.ctl, force, 0);
+    }
+    if (inc) {
+        k_inc_split<<<B.inc_blocks, INC_TPB, 0, s>>>(B.kin, B.skeys, P.N, B.inc_cnt, B.inc_u, B.inc_k[0],
+                                                     B.inc_i[0] + 0, B.ctl);
+        // the changed keys: stable radix sort of (key, index), lane 1
+        int ib = (B.inc_max + TPB * 8 - 1) / (TPB * 8);
+        ib = ib < 1 ? 1 : (ib > 152 * 8 ? 152 * 8 : ib);
+        k_hist<<<ib, SORT_TPB, 0, s>>>(B.inc_k[0], B.inc_max, B.npasses, B.ctl, 0, 1);
+        const uint32_t* ki = B.inc_k[0];
+        const uint32_t* vi = B.inc_i[0];
+        for (int p = 0; p < B.npasses; ++p) {
+            uint32_t* ko = B.inc_k[(p + 1) & 1];
+            uint32_t* vo = B.inc_i[(p + 1) & 1];
+            k_radix_pass<<<B.inc_tiles, SORT_TPB, 0, s>>>(ki, vi, ko, vo, B.inc_status, B.inc_max, B.inc_tiles, p,
+                                                          B.ctl, 0, 1);
+            ki = ko;
+            vi = vo;
+        }
+        const int mb = (P.N + INC_TPB * MERGE_ITEMS - 1) / (INC_TPB * MERGE_ITEMS);
+        k_inc_merge<<<mb, INC_TPB, 0, s>>>(B.inc_u, B.kin, ki, vi, P.N, B.skeys, B.perm, B.ctl);
     }
 }
 

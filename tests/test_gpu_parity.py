@@ -470,3 +470,29 @@ def test_dense_window_stops_run():
     assert e.value.status == abi.ASPH_ERR_DENSE
     assert sim.control()["aborted"] == 1
     sim.close()
+
+
+# ---------------------------------------------------------------------------
+# incremental sort: a step whose keys mostly did not change sorts only the
+# changed ones and merges; the result is the stable sort of all keys
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("speed,shuffle", [(2.0, False), (40.0, False), (2.0, True)])
+def test_step_sort_is_the_stable_sort_of_its_keys(speed, shuffle):
+    p = small_config(sort_every=1)
+    s = random_state(p, 21, speed=speed, shuffle=True)
+    sim = _ctx(p, s)
+    if not shuffle:
+        sim.sort_build()          # start from sorted order: few keys change per step
+    changed = []
+    for _ in range(4):
+        pre = sim.get_sort()
+        kin = pre["keys_in"].copy()          # the keys this step sorts
+        sim.step(1)
+        srt = sim.get_sort()
+        ref = np.argsort(kin, kind="stable")
+        assert np.array_equal(srt["perm"], ref.astype(np.uint32))
+        assert np.array_equal(srt["keys_sorted"], kin[ref])
+        changed.append(np.count_nonzero(kin != pre["keys_sorted"]))
+    if not shuffle and speed < 10:
+        assert 0 < max(changed) < p.n_particles // 8    # the incremental path ran
+    sim.close()
