@@ -167,6 +167,65 @@ __device__ __forceinline__ void for_window_smem(const int* s_off, int lx, int ly
 }
 
 
+// Offsets of the staged region of a brick: s_off[l] = first slot of region
+// cell l (row-major, HALO cells around the brick, x/y wrapped), s_off[R] =
+// the total, s_start[l] = the cell's first global index, and (when it fits,
+// total <= cap) s_cell[k] = the region cell of slot k.  A cell's particles
+// take consecutive slots in index order.  The cell-table loads are strided
+// over the block with four in flight per thread; the scan runs in shared
+// memory.
+template <int BX, int BY, int BZ>
+__device__ int region_offsets(const Phys& P, const int2* __restrict__ range, int bxi, int byi, int bzi, int* s_off,
+                              int* s_start, unsigned short* s_cell, int cap, int* s_warp) {
+    using G = BrickGeom<BX, BY, BZ>;
+    const int T = blockDim.x;
+    const int rx0 = bxi * BX - HALO, ry0 = byi * BY - HALO, rz0 = bzi * BZ - HALO;
+    for (int lb = threadIdx.x; lb < G::R; lb += 4 * T) {
+        int2 rg[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int l = lb + u * T;
+            rg[u] = make_int2(0, 0);
+            if (l < G::R) {
+                const int lx = l % G::RX, ly = (l / G::RX) % G::RY, lz = l / (G::RX * G::RY);
+                const int gz = rz0 + lz;
+                if (gz >= 0 && gz < P.nz) {
+                    int gx = rx0 + lx, gy = ry0 + ly;
+                    gx += gx < 0 ? P.nx : 0; gx -= gx >= P.nx ? P.nx : 0;
+                    gy += gy < 0 ? P.ny : 0; gy -= gy >= P.ny ? P.ny : 0;
+                    rg[u] = range[(size_t)(gz * P.ny + gy) * P.nx + gx];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int l = lb + u * T;
+            if (l < G::R) {
+                s_start[l] = rg[u].x;
+                s_off[l] = rg[u].y - rg[u].x;
+            }
+        }
+    }
+    __syncthreads();
+    const int chunk = (G::R + T - 1) / T;
+    const int l0 = threadIdx.x * chunk, l1 = min(l0 + chunk, G::R);
+    int run = 0;
+    for (int l = l0; l < l1; ++l) run += s_off[l];
+    int total;
+    int excl = block_excl_scan_int(run, s_warp, &total);
+    const bool map = total <= cap;
+    for (int l = l0; l < l1; ++l) {
+        const int c = s_off[l];
+        s_off[l] = excl;
+        if (map)
+            for (int k = 0; k < c; ++k) s_cell[excl + k] = (unsigned short)l;
+        excl += c;
+    }
+    if (threadIdx.x == 0) s_off[G::R] = total;
+    __syncthreads();
+    return total;
+}
+
 // Neighbour-list writer of one target (slot-major, coalesced over targets).
 struct NbrOut {
     int* nbr;
@@ -230,7 +289,8 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
     int* s_gidx = reinterpret_cast<int*>(sp + C.cap);                    // global index of a staged slot
     int* s_off = s_gidx + C.cap;                                         // R + 1
     int* s_start = s_off + (G::R + 1);                                   // R
-    // the drain queue reuses s_start, which is only needed while staging
+    unsigned short* s_cell = reinterpret_cast<unsigned short*>(s_start + G::R);   // cap: region cell of a slot
+    // the drain queue reuses s_start and s_cell, which are only needed while staging
     unsigned short* s_list = reinterpret_cast<unsigned short*>(s_start);      // DLIST x T
     __shared__ int s_warp[32];
     __shared__ int s_span[2];
@@ -243,45 +303,31 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
     }
     const float dt = A.ctl->dt;
 
-    // ---- stage the region: counts, scan, copy (row-major by region cell)
-    const int rx0 = bxi * BX - HALO, ry0 = byi * BY - HALO, rz0 = bzi * BZ - HALO;
-    const int chunk = (G::R + T - 1) / T;
-    const int l0 = threadIdx.x * chunk, l1 = min(l0 + chunk, G::R);
-    int run = 0;
-    for (int l = l0; l < l1; ++l) {
-        const int lx = l % G::RX, ly = (l / G::RX) % G::RY, lz = l / (G::RX * G::RY);
-        const int gz = rz0 + lz;
-        int c = 0, st = 0;
-        if (gz >= 0 && gz < P.nz) {
-            int gx = rx0 + lx, gy = ry0 + ly;
-            gx += gx < 0 ? P.nx : 0; gx -= gx >= P.nx ? P.nx : 0;
-            gy += gy < 0 ? P.ny : 0; gy -= gy >= P.ny ? P.ny : 0;
-            const int2 rg = A.range[(size_t)(gz * P.ny + gy) * P.nx + gx];
-            st = rg.x;
-            c = rg.y - rg.x;
-        }
-        s_start[l] = st;
-        s_off[l] = c;
-        run += c;
-    }
-    int total;
-    int excl = block_excl_scan_int(run, s_warp, &total);
-    for (int l = l0; l < l1; ++l) {
-        const int c = s_off[l];
-        s_off[l] = excl;
-        excl += c;
-    }
-    if (threadIdx.x == 0) s_off[G::R] = total;
-    __syncthreads();
+    // ---- stage the region: counts, scan (row-major by region cell), copy
+    const int total = region_offsets<BX, BY, BZ>(P, A.range, bxi, byi, bzi, s_off, s_start, s_cell, C.cap, s_warp);
     const bool staged = total <= C.cap;
     if (staged) {
-        for (int l = l0; l < l1; ++l) {
-            const int o = s_off[l], c = s_off[l + 1] - o, st = s_start[l];
-            for (int k = 0; k < c; ++k) {
-                const float4 q = A.pos[st + k];
-                const float3 u = to_cells(P, q.x, q.y, q.z);   // compared in cell units
-                sp[o + k] = make_float4(u.x, u.y, u.z, q.w);
-                s_gidx[o + k] = st + k;
+        // slots strided over the block, four loads in flight per thread
+        for (int kb = threadIdx.x; kb < total; kb += 4 * T) {
+            float4 q[4];
+            int jg[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int k = kb + u * T;
+                if (k < total) {
+                    const int l = s_cell[k];
+                    jg[u] = s_start[l] + (k - s_off[l]);
+                    q[u] = A.pos[jg[u]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int k = kb + u * T;
+                if (k < total) {
+                    const float3 c = to_cells(P, q[u].x, q[u].y, q[u].z);   // compared in cell units
+                    sp[k] = make_float4(c.x, c.y, c.z, q[u].w);
+                    s_gidx[k] = jg[u];
+                }
             }
         }
     }
@@ -537,8 +583,10 @@ Launch plan(const Phys& P, const Shape& s) {
     // close to the mean), in whole warps, 64..512
     int t = (int)(s.bx * s.by * s.bz * ppc * 1.04 + 31) / 32 * 32;
     L.threads = t < 64 ? 64 : (t > 512 ? 512 : t);
-    const size_t queue = (size_t)DLIST * L.threads * 2, start = (size_t)4 * R;
-    L.smem = (size_t)L.C.cap * 16 + (size_t)L.C.cap * 4 + (size_t)4 * (R + 1) + (queue > start ? queue : start);
+    // s_start (R ints) and s_cell (cap shorts) while staging; the drain queue after
+    const size_t queue = (size_t)DLIST * L.threads * 2, start = (size_t)4 * R + (size_t)2 * L.C.cap;
+    L.smem = (size_t)L.C.cap * 16 + (size_t)L.C.cap * 4 + (size_t)4 * (R + 1) +
+             ((queue > start ? queue : start) + 15) / 16 * 16;
     return L;
 }
 
