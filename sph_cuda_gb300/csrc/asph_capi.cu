@@ -330,6 +330,7 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     AL(B.status, (size_t)B.npasses * B.ntiles * 256 * 8);
     AL(B.range, C * 8); AL(B.surf, N); AL(B.rain_delta, C * 4); AL(B.precip, (size_t)P.nxy * 4);
     AL(B.ctl, sizeof(DevCtl));
+    AL(B.spans, (size_t)pair_max_bricks(P) * 8);
     AL(B.nbr, (size_t)NBR_CAP * N * 4);
     AL(B.nbr_cnt, N * 4);
     sort_inc_sizes(P.N, &B.inc_max, &B.inc_tiles, &B.inc_blocks);

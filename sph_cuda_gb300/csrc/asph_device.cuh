@@ -176,7 +176,7 @@ __device__ __forceinline__ void density_eos_epilogue(const Phys& P, const DOut& 
     const float pfl = fmaxf(snd_eval(P.snd_p, P.snd_n, z).v() + ppr, 1.0f);
     const float Pi = powf(pfl / P0, R_D / CP);
 
-    float4 t = O.thq[i];
+    const float4 t = O.thq[i];
     float th = t.x, qv = t.y, qc = t.z;
     float T = th * Pi;
     const float qs = qsat(T, pfl);

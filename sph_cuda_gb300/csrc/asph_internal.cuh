@@ -67,6 +67,7 @@ struct Bufs {
     float*  precip;     // accumulated surface precipitation [kg/m^2]
     DevCtl* ctl;
     float4* snd;        // sounding tables: rho_ref, pres_ref, thvr (3 x snd_n nodes)
+    int2*   spans;      // per brick of the density pass: its span of targets in the sorted order
     int*    nbr;        // neighbour lists of the density pass, slot-major [NBR_CAP][N]
     int*    nbr_cnt;    // neighbours per particle, -1 when the list overflowed
     int ntiles, npasses;
@@ -109,6 +110,8 @@ void launch_rain(const Phys& P, const Bufs& B, cudaStream_t s);
 // Brick shape index the density pass uses (-1: per-target global path),
 // the number of shapes, and whether shape k suits the grid and density.
 int pair_shape(const Phys& P, const Bufs& B);
+// Most bricks any brick shape needs for this grid (sizes Bufs::spans).
+int pair_max_bricks(const Phys& P);
 int pair_shape_count();
 bool pair_shape_fits(const Phys& P, int k);
 void launch_cfl(const Phys& P, const Bufs& B, cudaStream_t s);

@@ -245,11 +245,26 @@ struct DArgs {
     const float4* pos;      // x, y, z, rho_old
     const int2* range;
     const uint32_t* skeys;  // sorted keys of the table's order
+    const int2* spans;      // per brick: its span of targets in the sorted order
     DOut out;
     int* nbr;
     int* nbr_cnt;
     DevCtl* ctl;
 };
+
+// Every brick's span of targets in the sorted order: the brick is a
+// Morton-aligned key range, found by binary search in the sorted keys (one
+// thread per brick, before the pass, so that no CTA of the pass waits on it).
+template <int BX, int BY, int BZ>
+__global__ void k_brick_spans(const __grid_constant__ Phys P, const uint32_t* __restrict__ skeys, int2* spans,
+                              PairCfg C, const DevCtl* __restrict__ ctl) {
+    using G = BrickGeom<BX, BY, BZ>;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= C.nbricks || ctl->aborted) return;
+    const int bxi = b % C.nbx, byi = (b / C.nbx) % C.nby, bzi = b / (C.nbx * C.nby);
+    const uint32_t base = morton3((uint32_t)(bxi * BX), (uint32_t)(byi * BY), (uint32_t)(bzi * BZ));
+    spans[b] = make_int2(lower_bound_u32(skeys, P.N, base), lower_bound_u32(skeys, P.N, base + (uint32_t)G::KEYS));
+}
 
 // Out of line: only targets that leave the staged region come here, and
 // keeping it out of the brick kernel keeps that kernel free of spills.
@@ -297,9 +312,10 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
     if (A.ctl->aborted) return;
     const int b = blockIdx.x;
     const int bxi = b % C.nbx, byi = (b / C.nbx) % C.nby, bzi = b / (C.nbx * C.nby);
-    if (threadIdx.x < 2) {
-        const uint32_t base = morton3((uint32_t)(bxi * BX), (uint32_t)(byi * BY), (uint32_t)(bzi * BZ));
-        s_span[threadIdx.x] = lower_bound_u32(A.skeys, P.N, base + (threadIdx.x ? (uint32_t)G::KEYS : 0u));
+    if (threadIdx.x == 0) {
+        const int2 sp2 = A.spans[b];
+        s_span[0] = sp2.x;
+        s_span[1] = sp2.y;
     }
     const float dt = A.ctl->dt;
 
@@ -593,6 +609,8 @@ Launch plan(const Phys& P, const Shape& s) {
 template <int BX, int BY, int BZ>
 void launch_d(const Phys& P, const DArgs& A, cudaStream_t s) {
     const Launch L = plan(P, Shape{BX, BY, BZ});
+    k_brick_spans<BX, BY, BZ><<<(L.C.nbricks + 255) / 256, 256, 0, s>>>(P, A.skeys, const_cast<int2*>(A.spans), L.C,
+                                                                        A.ctl);
     cudaFuncSetAttribute(k_density_brick<BX, BY, BZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
     k_density_brick<BX, BY, BZ><<<L.C.nbricks, L.threads, L.smem, s>>>(P, A, L.C);
 }
@@ -602,6 +620,14 @@ inline int blocks_for(int n, int tpb) { return n <= 0 ? 1 : (n + tpb - 1) / tpb;
 }  // namespace
 
 int pair_shape(const Phys& P, const Bufs& B) { return shape_in_use(P, B); }
+int pair_max_bricks(const Phys& P) {
+    int m = 1;
+    for (const Shape& sh : SHAPES) {
+        const int n = ((P.nx + sh.bx - 1) / sh.bx) * ((P.ny + sh.by - 1) / sh.by) * ((P.nz + sh.bz - 1) / sh.bz);
+        m = n > m ? n : m;
+    }
+    return m;
+}
 int pair_shape_count() { return (int)(sizeof(SHAPES) / sizeof(SHAPES[0])); }
 bool pair_shape_fits(const Phys& P, int k) { return k >= 0 && k < pair_shape_count() && fits(P, k); }
 
@@ -615,6 +641,7 @@ void launch_density(const Phys& P, const Bufs& B, cudaStream_t s) {
     const bool reads = P.accretion || P.rain_evap;
     A.out.rain_cur = B.rain[B.rc];
     A.out.rain_dep = reads ? B.rain_delta : B.rain[B.rc];
+    A.spans = B.spans;
     A.nbr = B.nbr;
     A.nbr_cnt = B.nbr_cnt;
     A.ctl = B.ctl;
