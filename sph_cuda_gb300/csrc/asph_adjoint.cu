@@ -324,13 +324,13 @@ __global__ void k_adj_mom_seed(const Phys P, float dt, StepTape T, AdjBufs A) {
 // R5b: momentum pair sums.  For the pair (i, j) in i's list, the thread of
 // i takes the derivative of i's own pair term (seeds of i) and of the term
 // i contributes to j's sum (seeds of j) with respect to i's variables.
-__global__ __launch_bounds__(ATPB) void k_adj_mom_pairs(const Phys P, StepTape T, AdjBufs A) {
+__global__ __launch_bounds__(ATPB, 4) void k_adj_mom_pairs(const Phys P, StepTape T, AdjBufs A) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float la = 0.f, lb = 0.f;
     if (i < P.N) {
         const float4 xi = T.pos1[i], vi = T.vel1[i], sFi = A.sF[i], sVi = A.sV[i];
         const float2 ri = T.rp[i];
-        const float rhoi = fmaxf(ri.x, 1e-3f), iri = 1.f / rhoi;
+        const float rhoi = fmaxf(ri.x, 1e-3f), iri = __fdividef(1.f, rhoi);
         const float Ii = ri.x > 1e-3f ? 1.f : 0.f;
         const int cnt = T.cnt[i];
         if (cnt < 0) atomicExch(A.err, 1);   // list overflow: the adjoint needs every pair
@@ -341,91 +341,67 @@ __global__ __launch_bounds__(ATPB) void k_adj_mom_pairs(const Phys P, StepTape T
             const int j = T.lst[(size_t)q * P.N + i];
             const float4 xj = T.pos1[j], vj = T.vel1[j], sFj = A.sF[j], sVj = A.sV[j];
             const float2 rj = T.rp[j];
-            if (r2_cells(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z) >= 4.f) continue;   // the pass's own test
+            // the pair geometry exactly as the forward pass forms it (msum_add)
             const float rx = xi.x - xj.x, ry = xi.y - xj.y, rz = xi.z - xj.z;
             const float dxt = rx * P.inv_dx, dyt = ry * P.inv_dy, dzt = rz * P.inv_dz;
-            const float r2t = dxt * dxt + dyt * dyt + dzt * dzt;
-            if (r2t >= 4.f || r2t < 1e-12f) continue;
-            const float qq = sqrtf(r2t);
-            float kq, kp;   // W'(q)/q and d/dq of it
-            if (qq < 1.f) {
-                kq = SIGMA_W * (2.25f * qq - 3.f);
-                kp = SIGMA_W * 2.25f;
-            } else {
-                const float t2 = 2.f - qq;
-                kq = -0.75f * SIGMA_W * t2 * t2 / qq;
-                kp = 0.75f * SIGMA_W * t2 * (qq + 2.f) / (qq * qq);
-            }
-            const float kpq = kp / qq;
+            const float r2t = __fmaf_rn(dxt, dxt, __fmaf_rn(dyt, dyt, dzt * dzt));
+            if (r2t < 1e-12f) continue;
+            const float rs = rsqrtf(r2t);
+            const float qq = r2t * rs;
+            const float t2 = 2.f - qq;
+            // W'(q)/q and its q-derivative (both branches as in the forward)
+            const float kq = qq < 1.f ? SIGMA_W * __fmaf_rn(2.25f, qq, -3.f) : (-0.75f * SIGMA_W) * (t2 * t2) * rs;
+            const float kpq = qq < 1.f ? (2.25f * SIGMA_W) * rs : (0.75f * SIGMA_W) * t2 * (qq + 2.f) * (rs * rs * rs);
             const float Mrx = Mx * rx, Mry = My * ry, Mrz = Mz * rz;   // M r
             const float gxx = kq * Mrx, gyy = kq * Mry, gzz = kq * Mrz;   // grad_i W
-            const float rhoj = fmaxf(rj.x, 1e-3f), irj = 1.f / rhoj;
-            const float dp = (rj.y - ri.y) * iri * irj;   // dp_ij ; dp_ji = -dp
+            const float rhoj = fmaxf(rj.x, 1e-3f), irj = __fdividef(1.f, rhoj);
+            const float dp = (rj.y - ri.y) * (iri * irj);   // dp_ij ; dp_ji = -dp
             const float ux = vi.x - vj.x, uy = vi.y - vj.y, uz = vi.z - vj.z;
-            const float s = ux * rx + uy * ry + uz * rz;
-            float mu = 0.f, den = 1.f, rbar = 0.5f * (rhoi + rhoj), Phi = 0.f, dPhi = 0.f;
-            const bool vis = s < 0.f;
+            const float sdot = __fmaf_rn(ux, rx, __fmaf_rn(uy, ry, uz * rz));
+            float mu = 0.f, hd = 0.f, m2 = 0.f, Phi = 0.f, dPhi = 0.f;
+            const float rbar = 0.5f * (rhoi + rhoj), irb = __fdividef(1.f, rbar), ir2 = irb * irb;
+            const bool vis = sdot < 0.f;
             if (vis) {
-                den = rx * rx + ry * ry + rz * rz + P.eta2;
-                mu = P.h_av * s / den;
-                Phi = -P.alpha * P.cs * mu + P.beta * mu * mu;
-                dPhi = -P.alpha * P.cs + 2.f * P.beta * mu;
+                const float iden = __fdividef(1.f, __fmaf_rn(rx, rx, __fmaf_rn(ry, ry, rz * rz)) + P.eta2);
+                hd = P.h_av * iden;
+                mu = hd * sdot;
+                m2 = 2.f * mu * iden;
+                Phi = mu * __fmaf_rn(P.beta, mu, -P.alpha * P.cs);
+                dPhi = __fmaf_rn(2.f * P.beta, mu, -P.alpha * P.cs);
             }
-            const float ir2 = 1.f / (rbar * rbar);
-            const float visc_ij = Phi * irj * ir2;   // in i's sum
-            const float visc_ji = Phi * iri * ir2;   // in j's sum
-            Vx -= visc_ij * gxx; Vy -= visc_ij * gyy; Vz -= visc_ij * gzz;
-            // ---- (a) i's own term, seeds of i
-            {
-                const float Aa = sFi.x * gxx + sFi.y * gyy + sFi.z * gzz;
-                const float Bv = sVi.x * gxx + sVi.y * gyy + sVi.z * gzz;
-                const float br = dp + visc_ij;
-                const float cx = -br * sFi.x - visc_ij * sVi.x, cy = -br * sFi.y - visc_ij * sVi.y,
-                            cz = -br * sFi.z - visc_ij * sVi.z;   // dc/dg
-                const float rMc = rx * Mx * cx + ry * My * cy + rz * Mz * cz;
-                gx += kq * Mx * cx + kpq * rMc * Mrx;
-                gy += kq * My * cy + kpq * rMc * Mry;
-                gz += kq * Mz * cz + kpq * rMc * Mrz;
-                gP += Aa * iri * irj;
-                grho += Ii * Aa * dp * iri;
-                if (vis) {
-                    const float Psi = -(Aa + Bv);
-                    const float lmu = Psi * dPhi * irj * ir2;
-                    const float hd = P.h_av / den, m2 = 2.f * mu / den;
-                    gvx += lmu * hd * rx; gvy += lmu * hd * ry; gvz += lmu * hd * rz;
-                    gx += lmu * (hd * ux - m2 * rx);
-                    gy += lmu * (hd * uy - m2 * ry);
-                    gz += lmu * (hd * uz - m2 * rz);
-                    grho += Ii * Psi * (-visc_ij / rbar);   // rbar = (rho_i + rho_j)/2
-                    la += Psi * (-P.cs * mu) * irj * ir2;
-                    lb += Psi * (mu * mu) * irj * ir2;
-                }
-            }
-            // ---- (b) the term of j's sum in which i is the neighbour, seeds of j
-            {
-                const float Aa = -(sFj.x * gxx + sFj.y * gyy + sFj.z * gzz);   // sF_j . g_ji, g_ji = -g_ij
-                const float Bv = -(sVj.x * gxx + sVj.y * gyy + sVj.z * gzz);
-                const float br = -dp + visc_ji;
-                const float cx = -br * sFj.x - visc_ji * sVj.x, cy = -br * sFj.y - visc_ji * sVj.y,
-                            cz = -br * sFj.z - visc_ji * sVj.z;   // dc/dg_ji
-                const float rMc = rx * Mx * cx + ry * My * cy + rz * Mz * cz;
-                // dc/dr_ji = kq M c + kpq (r.Mc) M r ; dc/dx_i = -dc/dr_ji
-                gx -= kq * Mx * cx + kpq * rMc * Mrx;
-                gy -= kq * My * cy + kpq * rMc * Mry;
-                gz -= kq * Mz * cz + kpq * rMc * Mrz;
-                gP -= Aa * irj * iri;
-                grho += Ii * Aa * (-dp) * iri;
-                if (vis) {
-                    const float Psi = -(Aa + Bv);
-                    const float lmu = Psi * dPhi * iri * ir2;
-                    const float hd = P.h_av / den, m2 = 2.f * mu / den;
-                    gvx += lmu * hd * rx; gvy += lmu * hd * ry; gvz += lmu * hd * rz;
-                    gx += lmu * (hd * ux - m2 * rx);
-                    gy += lmu * (hd * uy - m2 * ry);
-                    gz += lmu * (hd * uz - m2 * rz);
-                    // visc_ji = Phi / (rho_i rbar^2)
-                    grho += Ii * Psi * (-visc_ji) * (iri + 1.f / rbar);
-                }
+            const float visc_ij = Phi * (irj * ir2);   // in i's sum
+            const float visc_ji = Phi * (iri * ir2);   // in j's sum
+            Vx = __fmaf_rn(-visc_ij, gxx, Vx); Vy = __fmaf_rn(-visc_ij, gyy, Vy); Vz = __fmaf_rn(-visc_ij, gzz, Vz);
+            // ---- (a) i's own term, seeds of i; (b) the term of j's sum in which i is
+            // the neighbour, seeds of j (g_ji = -g_ij, dp_ji = -dp).  Both give
+            // dc/dx_i = +-(kq M c + kpq (r.Mc) M r) with c = dc/dg.
+            const float Aa = __fmaf_rn(sFi.x, gxx, __fmaf_rn(sFi.y, gyy, sFi.z * gzz));
+            const float Ba = __fmaf_rn(sVi.x, gxx, __fmaf_rn(sVi.y, gyy, sVi.z * gzz));
+            const float Ab = -__fmaf_rn(sFj.x, gxx, __fmaf_rn(sFj.y, gyy, sFj.z * gzz));
+            const float Bb = -__fmaf_rn(sVj.x, gxx, __fmaf_rn(sVj.y, gyy, sVj.z * gzz));
+            const float bra = dp + visc_ij, brb = visc_ji - dp;
+            // c_a - c_b (the x_i derivative of (b) enters with a minus sign)
+            const float cx = -bra * sFi.x - visc_ij * sVi.x + brb * sFj.x + visc_ji * sVj.x;
+            const float cy = -bra * sFi.y - visc_ij * sVi.y + brb * sFj.y + visc_ji * sVj.y;
+            const float cz = -bra * sFi.z - visc_ij * sVi.z + brb * sFj.z + visc_ji * sVj.z;
+            const float rMc = __fmaf_rn(Mrx, cx, __fmaf_rn(Mry, cy, Mrz * cz));
+            gx += __fmaf_rn(kq * Mx, cx, kpq * rMc * Mrx);
+            gy += __fmaf_rn(kq * My, cy, kpq * rMc * Mry);
+            gz += __fmaf_rn(kq * Mz, cz, kpq * rMc * Mrz);
+            gP += (Aa - Ab) * (iri * irj);
+            grho += Ii * (Aa - Ab) * dp * iri;
+            if (vis) {
+                const float Psa = -(Aa + Ba), Psb = -(Ab + Bb);
+                const float lmu = dPhi * ir2 * (Psa * irj + Psb * iri);
+                gvx = __fmaf_rn(lmu * hd, rx, gvx); gvy = __fmaf_rn(lmu * hd, ry, gvy); gvz = __fmaf_rn(lmu * hd, rz, gvz);
+                gx = __fmaf_rn(lmu, __fmaf_rn(hd, ux, -m2 * rx), gx);
+                gy = __fmaf_rn(lmu, __fmaf_rn(hd, uy, -m2 * ry), gy);
+                gz = __fmaf_rn(lmu, __fmaf_rn(hd, uz, -m2 * rz), gz);
+                // visc_ij = Phi / (rho_j rbar^2), visc_ji = Phi / (rho_i rbar^2), rbar = (rho_i + rho_j)/2
+                grho += Ii * (Psa * (-visc_ij * irb) + Psb * (-visc_ji) * (iri + irb));
+                const float wa = Psa * (irj * ir2);
+                la = __fmaf_rn(wa, -P.cs * mu, la);
+                lb = __fmaf_rn(wa, mu * mu, lb);
             }
         }
         // heating: d dth / d v1 = -Vm / (cp Pi)
@@ -507,16 +483,18 @@ __global__ void k_adj_dens_a(const Phys P, StepTape T, AdjBufs A) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const float4 xi = T.pos1[i];
-    float S1 = w3(0.f), S2 = w3(0.f) / fmaxf(xi.w, 1e-3f);   // self pair
+    float S1 = w3(0.f), S2 = __fdividef(w3(0.f), fmaxf(xi.w, 1e-3f));   // self pair
     const int cnt = T.cnt[i];
     for (int q = 0; q < cnt; ++q) {
         const int j = T.lst[(size_t)q * P.N + i];
         const float4 xj = T.pos1[j];
-        const float r2t = r2_cells(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z);
+        const float r2t = r2_cells(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z);   // the density pass's own r^2
         if (r2t >= 4.f || r2t < 1e-12f) continue;
-        const float W = w3(sqrtf(r2t));
+        const float qq = r2t * rsqrtf(r2t), t = 2.f - qq;
+        const float W = qq < 1.f ? SIGMA_W * __fmaf_rn(qq * qq, __fmaf_rn(0.75f, qq, -1.5f), 1.f)
+                                 : (0.25f * SIGMA_W) * (t * t * t);
         S1 += W;
-        S2 += W / fmaxf(xj.w, 1e-3f);
+        S2 += __fdividef(W, fmaxf(xj.w, 1e-3f));
     }
     float4 lx = A.lx[i];
     const float lrho = lx.w;
@@ -543,7 +521,7 @@ __global__ __launch_bounds__(ATPB) void k_adj_dens_b(const Phys P, StepTape T, A
     if (i >= P.N) return;
     const float4 xi = T.pos1[i];
     const float2 lSi = A.lS[i];
-    const float roi = fmaxf(xi.w, 1e-3f), iroi = 1.f / roi;
+    const float roi = fmaxf(xi.w, 1e-3f), iroi = __fdividef(1.f, roi);
     const float Mx = P.inv_dx * P.inv_dx, My = P.inv_dy * P.inv_dy, Mz = P.inv_dz * P.inv_dz;
     float gx = 0.f, gy = 0.f, gz = 0.f;
     float lro = lSi.y * (-w3(0.f) * iroi * iroi);   // self pair in S2_i
@@ -552,15 +530,14 @@ __global__ __launch_bounds__(ATPB) void k_adj_dens_b(const Phys P, StepTape T, A
         const int j = T.lst[(size_t)q * P.N + i];
         const float4 xj = T.pos1[j];
         const float2 lSj = A.lS[j];
-        if (r2_cells(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z) >= 4.f) continue;   // the pass's own test
-        const float rx = xi.x - xj.x, ry = xi.y - xj.y, rz = xi.z - xj.z;
-        const float dxt = rx * P.inv_dx, dyt = ry * P.inv_dy, dzt = rz * P.inv_dz;
-        const float r2t = dxt * dxt + dyt * dyt + dzt * dzt;
+        const float r2t = r2_cells(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z);   // the density pass's own r^2
         if (r2t >= 4.f || r2t < 1e-12f) continue;
-        const float qq = sqrtf(r2t);
-        const float W = w3(qq);
-        const float kq = dw3(qq) / qq;
-        const float iroj = 1.f / fmaxf(xj.w, 1e-3f);
+        const float rx = xi.x - xj.x, ry = xi.y - xj.y, rz = xi.z - xj.z;
+        const float rs = rsqrtf(r2t), qq = r2t * rs, t = 2.f - qq;
+        const float W = qq < 1.f ? SIGMA_W * __fmaf_rn(qq * qq, __fmaf_rn(0.75f, qq, -1.5f), 1.f)
+                                 : (0.25f * SIGMA_W) * (t * t * t);
+        const float kq = qq < 1.f ? SIGMA_W * __fmaf_rn(2.25f, qq, -3.f) : (-0.75f * SIGMA_W) * (t * t) * rs;
+        const float iroj = __fdividef(1.f, fmaxf(xj.w, 1e-3f));
         const float c = (lSi.x + lSj.x) + lSi.y * iroj + lSj.y * iroi;
         gx += c * kq * Mx * rx;
         gy += c * kq * My * ry;
