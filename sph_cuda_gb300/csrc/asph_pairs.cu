@@ -143,30 +143,6 @@ __device__ __forceinline__ bool local_window(const Phys& P, int bxi, int byi, in
            zhi < G::RZ;
 }
 
-// Flattened walk of the 5 x 5 x (z rows) window inside the staged region.
-template <int BX, int BY, int BZ, class F>
-__device__ __forceinline__ void for_window_smem(const int* s_off, int lx, int ly, int zlo, int zhi, F&& f) {
-    using G = BrickGeom<BX, BY, BZ>;
-    int jz = zlo, jy = ly - STENCIL;
-    int la = (jz * G::RY + jy) * G::RX + lx - STENCIL;
-    int k = s_off[la], kend = s_off[la + 5];
-    for (;;) {
-        if (k < kend) {
-            f(k);
-            ++k;
-            continue;
-        }
-        if (++jy > ly + STENCIL) {
-            jy = ly - STENCIL;
-            if (++jz > zhi) break;
-        }
-        la = (jz * G::RY + jy) * G::RX + lx - STENCIL;
-        k = s_off[la];
-        kend = s_off[la + 5];
-    }
-}
-
-
 // Offsets of the staged region of a brick: s_off[l] = first slot of region
 // cell l (row-major, HALO cells around the brick, x/y wrapped), s_off[R] =
 // the total, s_start[l] = the cell's first global index, and (when it fits,
@@ -384,24 +360,35 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
         }                                                                             \
         n = 0;                                                                        \
     } while (0)
-        // flattened walk of the window rows in the staged region; the warp
-        // votes once per 8 steps, so queues drain at DLIST - 8
+        // flattened walk of the window rows in the staged region.  A step
+        // that finds its row finished moves to the next row and tests that
+        // row's first candidate in the same step, so rows cost no steps of
+        // their own (only empty rows do).  la = region cell of the row's
+        // first cell; rows advance by RX, planes by RX * RY.  The warp votes
+        // once per 8 steps, so queues drain at DLIST - 8.
         bool done = !fast;
-        int jz = zlo, jy = ly - STENCIL, k = 0, kend = 0;
-        if (!done) row_span(s_off, (jz * G::RY + jy) * G::RX + lx - STENCIL, k, kend);
+        int la = (zlo * G::RY + ly - STENCIL) * G::RX + lx - STENCIL;
+        const int la_end = la + (zhi - zlo + 1) * (G::RX * G::RY);
+        int cy = 0, k = 0, kend = 0;
+        if (!done) row_span(s_off, la, k, kend);
         for (;;) {
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
                 if (!done) {
+                    if (k >= kend) {
+                        la += G::RX;
+                        if (++cy == 2 * STENCIL + 1) {
+                            cy = 0;
+                            la += G::RX * G::RY - (2 * STENCIL + 1) * G::RX;
+                        }
+                        if (la >= la_end) done = true;
+                        else row_span(s_off, la, k, kend);
+                    }
                     if (k < kend) {
                         const float4 pj = sp[k];
                         if (r2_scaled(ci.x, ci.y, ci.z, pj.x, pj.y, pj.z) < 4.0f)
                             s_list[(n++) * T + threadIdx.x] = (unsigned short)k;
                         ++k;
-                    } else if (++jy > ly + STENCIL && (jy = ly - STENCIL, ++jz > zhi)) {
-                        done = true;
-                    } else {
-                        row_span(s_off, (jz * G::RY + jy) * G::RX + lx - STENCIL, k, kend);
                     }
                 }
             }
