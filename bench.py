@@ -102,16 +102,6 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def launches_per_step(p) -> int:
-    """Kernels of one step: sort preparation, histogram, one radix pass per
-    8 key bits (3 bits per level of the largest axis), gather, density,
-    momentum."""
-    bits = 1
-    while (1 << bits) < max(p.nx, p.ny, p.nz):
-        bits += 1
-    return 5 + (3 * bits + 7) // 8
-
-
 def job_rate(units: float, seconds_local: float, dist=None, device="cpu"):
     """Whole-job throughput of independent replicas: every rank processes
     `units` inside its own timed region and the job time is the maximum over
@@ -227,8 +217,8 @@ def run_ours(args):
     N, C = p.n_particles, p.nx * p.ny * p.nz
     sim = sph.Asph(p, stream=stream.cuda_stream)
     sim.init()
-    per_step = launches_per_step(p)
     sim.step(max(args.warmup, 1))
+    per_step = sim.step_kernels()   # kernel nodes of the step's CUDA graph
 
     def barrier():
         if dist is not None:
@@ -328,7 +318,7 @@ def run_ours(args):
             "gpu_launches": per_step * args.steps,
             "clocks": clk,
             "state": {"simt": ctl["simt"], "steps_done": ctl["step"], "aborted": ctl["aborted"],
-                      "wmax": ctl["wmax"]},
+                      "wmax": ctl["wmax"], "deferred_targets_last_step": ctl["deferred"]},
         }
         print(json.dumps(line))
     sim.close()
@@ -370,6 +360,7 @@ def run_ensemble(args):
     views = [ens.member(k) for k in range(len(members))]
     for v in views:
         v.step(1)
+    member_kernels = sum(v.step_kernels() for v in views)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for v in views:
@@ -393,7 +384,7 @@ def run_ensemble(args):
                                                                for s in sorted(set(c[0] for c in chosen))},
                    "chosen_sort_counts": {str(s): sum(1 for c in chosen if c[1] == s)
                                           for s in sorted(set(c[1] for c in chosen))}},
-        "gpu_launches": args.steps * sum(launches_per_step(p) for p in members),
+        "gpu_launches": args.steps * member_kernels,
         "clocks": clk,
     }
     print(json.dumps(line))

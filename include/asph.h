@@ -137,6 +137,8 @@ typedef struct AsphControl {
     int32_t do_sort;        /* the next step starts with a sort */
     int32_t error;          /* device error word (ASPH_ERR_TIMEOUT ...) */
     int32_t surf_count;     /* particles in the lowest layer at the last sort */
+    int32_t deferred;       /* targets the last brick density pass left to its
+                               warp-per-target kernel (outside the staged bricks) */
 } AsphControl;
 
 /* ---- library / parameters ---------------------------------------------- */
@@ -201,6 +203,9 @@ int asph_step(asph_ctx* ctx, int nsteps);
 /* Queue nsteps without waiting; asph_sync() collects the status. */
 int asph_step_async(asph_ctx* ctx, int nsteps);
 int asph_sync(asph_ctx* ctx);
+/* Kernel launches of one step: the kernel nodes of the step's CUDA graph
+ * (captured here, without running, if no step ran yet). */
+int asph_step_kernels(asph_ctx* ctx, int* n);
 
 /* nsteps steps launched without a graph, with CUDA events between the
  * phases (the reference's per-phase timers, asph_h100.cu:931-954, 1149-1157).
@@ -214,7 +219,9 @@ int asph_step_profiled(asph_ctx* ctx, int nsteps, float* phase_ms);
 /* Execution options (setting one drops the captured step graphs).
  * ASPH_OPT_PAIR_PATH: 0 = automatic (brick-staged shared-memory pair
  * kernels where the grid allows), 1 = per-target global path everywhere
- * (same results to rounding; for testing).
+ * (same results to rounding; for testing), 2 = the density pass takes one
+ * warp per target for every target (the kernel that serves targets outside
+ * the staged bricks; same pairs, in the reference's order).
  * ASPH_OPT_PAIR_SHAPE: brick shape of the density pass, 0 = 8x8x8,
  * 1 = 8x8x4, 2 = 8x4x4, 3 = 4x4x4 cells, -1 = automatic (set); get returns
  * the shape in use, -1 for the global path.  A shape whose staged region

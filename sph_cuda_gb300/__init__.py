@@ -194,15 +194,22 @@ class Asph:
     def step_async(self, nsteps: int = 1) -> None:
         _check(self.lib.asph_step_async(self._ctx, int(nsteps)))
 
+    def step_kernels(self) -> int:
+        """Kernel launches of one step (kernel nodes of the step's CUDA graph)."""
+        n = C.c_int(0)
+        _check(self.lib.asph_step_kernels(self._ctx, C.byref(n)))
+        return int(n.value)
+
     def step_profiled(self, nsteps: int = 1) -> dict:
         """Per-phase device milliseconds summed over nsteps (non-graph launches)."""
         out = np.zeros(abi.NPHASES, np.float32)
         _check(self.lib.asph_step_profiled(self._ctx, int(nsteps), _fptr(out)))
         return dict(zip(abi.PHASES, out.tolist()))
 
-    def set_pair_path(self, global_path: bool) -> None:
-        """Force the per-target global pair path (True) or automatic (False)."""
-        _check(self.lib.asph_set_option(self._ctx, abi.OPT_PAIR_PATH, int(bool(global_path))))
+    def set_pair_path(self, global_path) -> None:
+        """Pair path: False/0 automatic, True/1 the per-target global path,
+        2 density with one warp per target."""
+        _check(self.lib.asph_set_option(self._ctx, abi.OPT_PAIR_PATH, int(global_path)))
 
     def pair_shape(self) -> int:
         v = C.c_int()

@@ -93,7 +93,7 @@ class AsphControl(C.Structure):
         ("dt", _f), ("dt_cap", _f), ("dt_floor", _f), ("dt_static", _f), ("dt_required", _f), ("sort_dt", _f),
         ("umax", _f), ("vmax", _f), ("wmax", _f),
         ("step", _i), ("trips", _i), ("sort_count", _i), ("aborted", _i), ("clamp_pending", _i),
-        ("do_sort", _i), ("error", _i), ("surf_count", _i),
+        ("do_sort", _i), ("error", _i), ("surf_count", _i), ("deferred", _i),
     ]
 
 
@@ -125,6 +125,7 @@ SIGNATURES = {
     "asph_cfl": (C.c_int, [_P]),
     "asph_step": (C.c_int, [_P, C.c_int]),
     "asph_step_async": (C.c_int, [_P, C.c_int]),
+    "asph_step_kernels": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "asph_sync": (C.c_int, [_P]),
     "asph_step_profiled": (C.c_int, [_P, C.c_int, _FP]),
     "asph_set_option": (C.c_int, [_P, C.c_int, C.c_int]),

@@ -333,6 +333,7 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     AL(B.spans, (size_t)pair_max_bricks(P) * 8);
     AL(B.nbr, (size_t)NBR_CAP * N * 4);
     AL(B.nbr_cnt, N * 4);
+    AL(B.defer, N * 4);
     sort_inc_sizes(P.N, &B.inc_max, &B.inc_tiles, &B.inc_blocks);
     AL(B.inc_u, N * 4);
     for (int k = 0; k < 2; ++k) {
@@ -402,7 +403,8 @@ int asph::sync_status(asph_ctx* c) {
 extern "C" int asph_set_option(asph_ctx* c, int option, int value) {
     if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
     if (option == ASPH_OPT_PAIR_PATH) {
-        if (value < 0 || value > 1) return fail(ASPH_ERR_ARG, "pair path must be 0 (auto) or 1 (global)");
+        if (value < 0 || value > 2)
+            return fail(ASPH_ERR_ARG, "pair path must be 0 (auto), 1 (global) or 2 (warp per target)");
         c->B.force_global = value;
     } else if (option == ASPH_OPT_PAIR_SHAPE) {
         if (value != -1 && !pair_shape_fits(c->P, value))
@@ -713,6 +715,7 @@ extern "C" int asph_get_control(asph_ctx* c, AsphControl* o) {
     o->umax = h.umax; o->vmax = h.vmax; o->wmax = h.wmax;
     o->step = h.step; o->trips = h.trips; o->sort_count = h.sort_count; o->aborted = h.aborted;
     o->clamp_pending = h.clamp_pending; o->do_sort = h.do_sort; o->error = h.error; o->surf_count = h.surf_count;
+    o->deferred = (int32_t)h.defer_n;
     return ASPH_OK;
 }
 
@@ -898,22 +901,53 @@ extern "C" int asph_step_profiled(asph_ctx* c, int nsteps, float* phase_ms) {
 
 int asph::graph_slot(const Bufs& B) { return B.pc | (B.vc << 1) | (B.qc << 2) | (B.rc << 3); }
 
+// Capture the step that starts from the current ping-pong state into its
+// graph (the indices are left as they were); counts the graph's kernels.
+static int capture_step_graph(asph_ctx* c, int slot) {
+    const Bufs saved = c->B;
+    cudaGraph_t g = nullptr;
+    CKR(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(c);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    c->B = saved;
+    if (e != cudaSuccess) return fail(ASPH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    size_t nn = 0;
+    e = cudaGraphGetNodes(g, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (e == cudaSuccess && nn) e = cudaGraphGetNodes(g, nodes.data(), &nn);
+    int kernels = 0;
+    for (size_t k = 0; e == cudaSuccess && k < nn; ++k) {
+        cudaGraphNodeType t;
+        e = cudaGraphNodeGetType(nodes[k], &t);
+        kernels += (e == cudaSuccess && t == cudaGraphNodeTypeKernel) ? 1 : 0;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->gexec[slot], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(ASPH_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    c->graph_kernels = kernels;
+    return ASPH_OK;
+}
+
+extern "C" int asph_step_kernels(asph_ctx* c, int* n) {
+    if (!c || !n) return fail(ASPH_ERR_ARG, "NULL argument");
+    if (!c->initialised) return fail(ASPH_ERR_STATE, "step_kernels before init/set_state");
+    const int slot = graph_slot(c->B);
+    if (!c->gexec[slot]) {
+        const int st = capture_step_graph(c, slot);
+        if (st) return st;
+    }
+    *n = c->graph_kernels;
+    return ASPH_OK;
+}
+
 extern "C" int asph_step_async(asph_ctx* c, int nsteps) {
     if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
     if (!c->initialised) return fail(ASPH_ERR_STATE, "step before init/set_state");
     for (int k = 0; k < nsteps; ++k) {
         const int slot = graph_slot(c->B);
         if (!c->gexec[slot]) {
-            const Bufs saved = c->B;
-            cudaGraph_t g = nullptr;
-            CKR(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            enqueue_step(c);
-            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-            if (e != cudaSuccess) return fail(ASPH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-            e = cudaGraphInstantiate(&c->gexec[slot], g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) return fail(ASPH_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-            c->B = saved;
+            const int st = capture_step_graph(c, slot);
+            if (st) return st;
         }
         CKR(cudaGraphLaunch(c->gexec[slot], c->stream));
         c->B.pc ^= 1; c->B.qc ^= 1; c->B.rc ^= 1;   // vel flips twice per step

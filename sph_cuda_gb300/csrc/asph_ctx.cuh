@@ -18,6 +18,7 @@ struct asph_ctx {
     bool lists_valid = false;   // neighbour lists match the current positions
     // graphs keyed by the ping-pong state at the start of the step
     cudaGraphExec_t gexec[16] = {};
+    int graph_kernels = 0;      // kernel nodes of a captured step graph
     // staging for host <-> device SoA copies (16 floats per particle)
     float* stage = nullptr;
     // audit

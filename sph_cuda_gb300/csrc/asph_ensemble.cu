@@ -32,6 +32,7 @@ struct asph_snapshot {
     float2* rp = nullptr;
     float *dthdt = nullptr, *rain = nullptr, *precip = nullptr;
     uint32_t* kin = nullptr;
+    uint32_t* skeys = nullptr;
     uint8_t* surf = nullptr;
     int2* range = nullptr;
     DevCtl* ctl = nullptr;
@@ -45,24 +46,30 @@ namespace {
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // One copy per field group, in a fixed order shared by save, restore and
-// the restart file.
+// the restart file.  Besides the particle and grid state this holds what the
+// last sort left for the next step: the cell table, the surface flags and the
+// sorted keys (the next incremental sort takes the particles whose key still
+// equals its sorted key as an already sorted subsequence, and the density
+// pass finds its bricks' spans in them).
 struct Part {
     void* dev;      // context buffer
     void* snap;     // snapshot buffer
     size_t bytes;
 };
+constexpr int NPARTS = 12;
 
-int parts(asph_ctx* c, const asph_snapshot* s, Part out[11]) {
+int parts(asph_ctx* c, const asph_snapshot* s, Part out[NPARTS]) {
     const Bufs& B = c->B;
     const size_t N = (size_t)c->P.N, C = (size_t)c->P.ncell;
-    Part p[11] = {
+    Part p[NPARTS] = {
         {B.pos[B.pc], s->pos, N * 16},  {B.vel[B.vc], s->vel, N * 16}, {B.thq[B.qc], s->thq, N * 16},
         {B.acc, s->acc, N * 16},        {B.rp, s->rp, N * 8},         {B.dthdt, s->dthdt, N * 4},
-        {B.kin, s->kin, N * 4},         {B.surf, s->surf, N},         {B.range, s->range, C * 8},
-        {B.rain[B.rc], s->rain, C * 4}, {B.precip, s->precip, (size_t)c->P.nxy * 4},
+        {B.kin, s->kin, N * 4},         {B.skeys, s->skeys, N * 4},   {B.surf, s->surf, N},
+        {B.range, s->range, C * 8},     {B.rain[B.rc], s->rain, C * 4},
+        {B.precip, s->precip, (size_t)c->P.nxy * 4},
     };
     memcpy(out, p, sizeof(p));
-    return 11;
+    return NPARTS;
 }
 
 bool same_shape(const asph_ctx* c, const asph_snapshot* s) {
@@ -77,8 +84,8 @@ extern "C" int asph_snapshot_create(asph_ctx* c, asph_snapshot** out) {
     asph_snapshot* s = new asph_snapshot();
     s->N = c->P.N; s->ncell = c->P.ncell; s->nxy = c->P.nxy;
     const size_t N = (size_t)s->N, C = (size_t)s->ncell;
-    const size_t sizes[12] = {N * 16, N * 16, N * 16, N * 16, N * 8, N * 4, N * 4, N, C * 8, C * 4,
-                              (size_t)s->nxy * 4, sizeof(DevCtl)};
+    const size_t sizes[NPARTS + 1] = {N * 16, N * 16, N * 16, N * 16, N * 8, N * 4, N * 4, N * 4, N, C * 8,
+                                      C * 4, (size_t)s->nxy * 4, sizeof(DevCtl)};
     size_t total = 0;
     for (size_t b : sizes) total += align256(b);
     cudaError_t e = cudaMalloc(&s->mem, total);
@@ -88,10 +95,11 @@ extern "C" int asph_snapshot_create(asph_ctx* c, asph_snapshot** out) {
                     cudaGetErrorString(e));
     }
     char* q = (char*)s->mem;
-    void** dst[12] = {(void**)&s->pos, (void**)&s->vel, (void**)&s->thq,  (void**)&s->acc,
-                      (void**)&s->rp,  (void**)&s->dthdt, (void**)&s->kin, (void**)&s->surf,
-                      (void**)&s->range, (void**)&s->rain, (void**)&s->precip, (void**)&s->ctl};
-    for (int k = 0; k < 12; ++k) {
+    void** dst[NPARTS + 1] = {(void**)&s->pos,   (void**)&s->vel,   (void**)&s->thq,   (void**)&s->acc,
+                              (void**)&s->rp,    (void**)&s->dthdt, (void**)&s->kin,   (void**)&s->skeys,
+                              (void**)&s->surf,  (void**)&s->range, (void**)&s->rain,  (void**)&s->precip,
+                              (void**)&s->ctl};
+    for (int k = 0; k < NPARTS + 1; ++k) {
         *dst[k] = q;
         q += align256(sizes[k]);
     }
@@ -108,7 +116,7 @@ extern "C" int asph_snapshot_save(asph_ctx* c, asph_snapshot* s) {
     if (!c || !s) return fail(ASPH_ERR_ARG, "NULL argument");
     if (!same_shape(c, s)) return fail(ASPH_ERR_ARG, "snapshot was made for another particle count or grid");
     if (!c->initialised) return fail(ASPH_ERR_STATE, "snapshot before init/set_state");
-    Part p[11];
+    Part p[NPARTS];
     const int n = parts(c, s, p);
     for (int k = 0; k < n; ++k) CKR(cudaMemcpyAsync(p[k].snap, p[k].dev, p[k].bytes, cudaMemcpyDeviceToDevice, c->stream));
     CKR(cudaMemcpyAsync(s->ctl, c->B.ctl, sizeof(DevCtl), cudaMemcpyDeviceToDevice, c->stream));
@@ -118,7 +126,7 @@ extern "C" int asph_snapshot_save(asph_ctx* c, asph_snapshot* s) {
 extern "C" int asph_snapshot_restore(asph_ctx* c, const asph_snapshot* s) {
     if (!c || !s) return fail(ASPH_ERR_ARG, "NULL argument");
     if (!same_shape(c, s)) return fail(ASPH_ERR_ARG, "snapshot was made for another particle count or grid");
-    Part p[11];
+    Part p[NPARTS];
     const int n = parts(c, s, p);
     for (int k = 0; k < n; ++k) CKR(cudaMemcpyAsync(p[k].dev, p[k].snap, p[k].bytes, cudaMemcpyDeviceToDevice, c->stream));
     // the radix look-back epoch keeps growing (status words of later sorts carry larger epochs)
@@ -138,7 +146,7 @@ struct RestartHeader {
     int32_t n_particles, nx, ny, nz, params_size, ctl_bytes;
 };
 constexpr uint32_t RESTART_MAGIC = 0x41535052u;   // "RPSA" little-endian: ASPH restart
-constexpr uint32_t RESTART_VERSION = 1;
+constexpr uint32_t RESTART_VERSION = 2;   // 2: the sorted keys of the last sort are saved
 
 }  // namespace
 
@@ -159,7 +167,7 @@ extern "C" int asph_checkpoint_write(asph_ctx* c, const char* path) {
         RestartHeader h{RESTART_MAGIC, RESTART_VERSION, c->P.N, c->P.nx, c->P.ny, c->P.nz, (int)sizeof(AsphParams),
                         (int)offsetof(DevCtl, epoch)};
         bool ok = fwrite(&h, sizeof h, 1, f) == 1 && fwrite(&c->prm, sizeof(AsphParams), 1, f) == 1;
-        Part p[12];
+        Part p[NPARTS + 1];
         const int n = parts(c, s, p);
         p[n] = Part{nullptr, s->ctl, (size_t)offsetof(DevCtl, epoch)};
         for (int k = 0; k <= n && ok; ++k) {
@@ -194,7 +202,7 @@ extern "C" int asph_checkpoint_read(asph_ctx* c, const char* path) {
     asph_snapshot* s = nullptr;
     if (!st) st = asph_snapshot_create(c, &s);
     if (!st) {
-        Part p[12];
+        Part p[NPARTS + 1];
         const int n = parts(c, s, p);
         p[n] = Part{nullptr, s->ctl, (size_t)offsetof(DevCtl, epoch)};
         std::vector<char> host;

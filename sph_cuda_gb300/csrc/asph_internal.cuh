@@ -25,6 +25,7 @@ struct DevCtl {
     float umax, vmax, wmax;
     int step, trips, sort_count, aborted, clamp_pending, do_sort, error, surf_count;
     int sorted_this_step;
+    unsigned defer_n;          // targets queued for the density pass's deferred kernel
     unsigned gmax[3];          // float bits of |u|,|v|,|w| maxima (atomicMax)
     unsigned done;             // finished-block counter of the momentum pass
     unsigned epoch;            // radix look-back epoch
@@ -70,9 +71,10 @@ struct Bufs {
     int2*   spans;      // per brick of the density pass: its span of targets in the sorted order
     int*    nbr;        // neighbour lists of the density pass, slot-major [NBR_CAP][N]
     int*    nbr_cnt;    // neighbours per particle, -1 when the list overflowed
+    int*    defer;      // targets of the density pass left to its deferred kernel (N slots)
     int ntiles, npasses;
     int pc, vc, qc, rc; // current index of pos/vel/thq/rain ping-pong pairs
-    int force_global;   // 1: pair passes take the per-target global path
+    int force_global;   // 1: pair passes take the per-target global path, 2: density warp per target
     int shape;          // brick shape index of the density pass, -1: automatic
     float4* src;        // source-term hook: per-particle tendencies (theta, qv, qc), NULL when off
     float4* src_tmp;    // the tendencies in the order of the current step (written by the gather)

@@ -15,34 +15,41 @@
 // D, brick path.  One CTA per Morton-aligned brick of BX x BY x BZ cells;
 // the brick's targets are one contiguous span of the sorted order and the
 // block has about as many threads as a brick has targets.  The CTA copies
-// the particles of every table cell within HALO = 3 cells of the brick
-// (stencil 2 + 1 cell of drift since the sort) into shared memory, bucketed
-// row-major by region cell, so that each row of a target's 5 x 5 x 5 window
-// is one contiguous span of shared memory; each thread walks its target's
-// row spans in one flattened loop, queues accepted candidates in a small
-// per-thread list in shared memory, and drains the list (density sums +
-// neighbour-list writes) in uniform loops.  A target whose window leaves
-// the staged region (drift > 1 cell), or a brick whose region overflows the
-// staging capacity, takes the global path.
+// the particles of every table cell within H cells of the brick into shared
+// memory, bucketed row-major by region cell, so that each row of a target's
+// 5 x 5 x 5 window is one contiguous span of shared memory; each thread
+// walks its target's row spans in one flattened loop, queues accepted
+// candidates in a small per-thread list in shared memory, and drains the
+// list (density sums + neighbour-list writes) in uniform loops.  H = 2 (the
+// stencil) covers every target still in a cell of its brick; H = 3 also
+// covers one cell of drift since the sort.  A target whose window leaves
+// the staged region, or every target of a brick whose region overflows the
+// staging capacity, is queued for the deferred pass.
+//
+// Deferred pass.  One warp per queued target: the lanes read the window's
+// cell ranges from the global table in parallel and test the candidates 32
+// at a time in the reference's order, so the neighbour list comes out in
+// that order.
 //
 // Global path.  One thread per target walking the cell table in global
 // memory, the reference's loop structure; used for grids narrower than the
-// staged region, for the fallbacks above, and by M for a target whose list
-// overflowed or was not produced on the current positions.
+// staged region, and by M for a target whose list overflowed or was not
+// produced on the current positions.
 #include "asph_device.cuh"
 #include "../../include/asph.h"
 
 namespace asph {
 
-constexpr int HALO = 3;
+constexpr int MAX_HALO = 3;      // widest staged halo (cells around a brick)
 constexpr int DLIST = 24;        // queued accepted candidates per thread (D)
 constexpr int M_TPB = 256;
 
-template <int BX, int BY, int BZ>
+template <int BX, int BY, int BZ, int H>
 struct BrickGeom {
     static_assert((BX == BY && BY == BZ) || (BX == 2 * BY && BY == BZ) || (BX == BY && BX == 2 * BZ),
                   "brick must be a Morton-aligned key range");
-    static constexpr int RX = BX + 2 * HALO, RY = BY + 2 * HALO, RZ = BZ + 2 * HALO;
+    static_assert(H >= STENCIL && H <= MAX_HALO, "halo must cover the stencil");
+    static constexpr int RX = BX + 2 * H, RY = BY + 2 * H, RZ = BZ + 2 * H;
     static constexpr int R = RX * RY * RZ;
     static constexpr int KEYS = BX * BY * BZ;
 };
@@ -127,16 +134,16 @@ __device__ __forceinline__ void row_span(const int* s_off, int la_m2, int& k, in
 }
 
 // Region-local window of a target: returns false if it leaves the region.
-template <int BX, int BY, int BZ>
+template <int BX, int BY, int BZ, int H>
 __device__ __forceinline__ bool local_window(const Phys& P, int bxi, int byi, int bzi, float x, float y, float z,
                                              int& lx, int& ly, int& zlo, int& zhi) {
-    using G = BrickGeom<BX, BY, BZ>;
+    using G = BrickGeom<BX, BY, BZ, H>;
     const int ix = cell_ix(x, P.inv_dx, P.nx), iy = cell_ix(y, P.inv_dy, P.ny), iz = cell_ix(z, P.inv_dz, P.nz);
-    lx = ix - (bxi * BX - HALO);
+    lx = ix - (bxi * BX - H);
     lx += lx < 0 ? P.nx : 0; lx -= lx >= P.nx ? P.nx : 0;
-    ly = iy - (byi * BY - HALO);
+    ly = iy - (byi * BY - H);
     ly += ly < 0 ? P.ny : 0; ly -= ly >= P.ny ? P.ny : 0;
-    const int rz0 = bzi * BZ - HALO;
+    const int rz0 = bzi * BZ - H;
     zlo = max(iz - STENCIL, 0) - rz0;
     zhi = min(iz + STENCIL, P.nz - 1) - rz0;
     return lx >= STENCIL && lx < G::RX - STENCIL && ly >= STENCIL && ly < G::RY - STENCIL && zlo >= 0 &&
@@ -144,18 +151,18 @@ __device__ __forceinline__ bool local_window(const Phys& P, int bxi, int byi, in
 }
 
 // Offsets of the staged region of a brick: s_off[l] = first slot of region
-// cell l (row-major, HALO cells around the brick, x/y wrapped), s_off[R] =
+// cell l (row-major, H cells around the brick, x/y wrapped), s_off[R] =
 // the total, s_start[l] = the cell's first global index, and (when it fits,
 // total <= cap) s_cell[k] = the region cell of slot k.  A cell's particles
 // take consecutive slots in index order.  The cell-table loads are strided
 // over the block with four in flight per thread; the scan runs in shared
 // memory.
-template <int BX, int BY, int BZ>
+template <int BX, int BY, int BZ, int H>
 __device__ int region_offsets(const Phys& P, const int2* __restrict__ range, int bxi, int byi, int bzi, int* s_off,
                               int* s_start, unsigned short* s_cell, int cap, int* s_warp) {
-    using G = BrickGeom<BX, BY, BZ>;
+    using G = BrickGeom<BX, BY, BZ, H>;
     const int T = blockDim.x;
-    const int rx0 = bxi * BX - HALO, ry0 = byi * BY - HALO, rz0 = bzi * BZ - HALO;
+    const int rx0 = bxi * BX - H, ry0 = byi * BY - H, rz0 = bzi * BZ - H;
     for (int lb = threadIdx.x; lb < G::R; lb += 4 * T) {
         int2 rg[4];
 #pragma unroll
@@ -225,6 +232,7 @@ struct DArgs {
     DOut out;
     int* nbr;
     int* nbr_cnt;
+    int* defer;             // targets queued for the deferred pass (count in ctl->defer_n)
     DevCtl* ctl;
 };
 
@@ -233,18 +241,17 @@ struct DArgs {
 // thread per brick, before the pass, so that no CTA of the pass waits on it).
 template <int BX, int BY, int BZ>
 __global__ void k_brick_spans(const __grid_constant__ Phys P, const uint32_t* __restrict__ skeys, int2* spans,
-                              PairCfg C, const DevCtl* __restrict__ ctl) {
-    using G = BrickGeom<BX, BY, BZ>;
+                              PairCfg C, DevCtl* ctl) {
+    using G = BrickGeom<BX, BY, BZ, STENCIL>;
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b == 0) ctl->defer_n = 0;   // the deferred queue of the pass that follows
     if (b >= C.nbricks || ctl->aborted) return;
     const int bxi = b % C.nbx, byi = (b / C.nbx) % C.nby, bzi = b / (C.nbx * C.nby);
     const uint32_t base = morton3((uint32_t)(bxi * BX), (uint32_t)(byi * BY), (uint32_t)(bzi * BZ));
     spans[b] = make_int2(lower_bound_u32(skeys, P.N, base), lower_bound_u32(skeys, P.N, base + (uint32_t)G::KEYS));
 }
 
-// Out of line: only targets that leave the staged region come here, and
-// keeping it out of the brick kernel keeps that kernel free of spills.
-__device__ __noinline__ DSum density_target_global(const Phys& P, const DArgs& A, int i, float4 pi, FF rr) {
+__device__ __forceinline__ DSum density_target_global(const Phys& P, const DArgs& A, int i, float4 pi, FF rr) {
     DSum s{0.f, 0.f, 0.f};
     NbrOut L{A.nbr, 0, P.N, i};
     for_window_global(P, A.range, A.ctl, pi.x, pi.y, pi.z, [&](int j) {
@@ -270,10 +277,10 @@ __global__ __launch_bounds__(256) void k_density_global(const __grid_constant__ 
     density_eos_epilogue(P, A.out, i, pi, s, rr, dt);
 }
 
-template <int BX, int BY, int BZ>
+template <int BX, int BY, int BZ, int H>
 __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ Phys P, const __grid_constant__ DArgs A,
                                                        PairCfg C) {
-    using G = BrickGeom<BX, BY, BZ>;
+    using G = BrickGeom<BX, BY, BZ, H>;
     extern __shared__ __align__(16) unsigned char smem[];
     const int T = blockDim.x;
     float4* sp = reinterpret_cast<float4*>(smem);                       // x, y, z in cell units, rho_old
@@ -296,7 +303,7 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
     const float dt = A.ctl->dt;
 
     // ---- stage the region: counts, scan (row-major by region cell), copy
-    const int total = region_offsets<BX, BY, BZ>(P, A.range, bxi, byi, bzi, s_off, s_start, s_cell, C.cap, s_warp);
+    const int total = region_offsets<BX, BY, BZ, H>(P, A.range, bxi, byi, bzi, s_off, s_start, s_cell, C.cap, s_warp);
     const bool staged = total <= C.cap;
     if (staged) {
         // slots strided over the block, four loads in flight per thread
@@ -341,7 +348,16 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
             pi = A.pos[i];
             ci = to_cells(P, pi.x, pi.y, pi.z);
             rr = snd_eval(P.snd_rho, P.snd_n, pi.z);
-            fast = staged && local_window<BX, BY, BZ>(P, bxi, byi, bzi, pi.x, pi.y, pi.z, lx, ly, zlo, zhi);
+            fast = staged && local_window<BX, BY, BZ, H>(P, bxi, byi, bzi, pi.x, pi.y, pi.z, lx, ly, zlo, zhi);
+        }
+        // targets the staged region does not cover go to the deferred pass
+        const unsigned dm = __ballot_sync(0xffffffffu, active && !fast);
+        if (dm) {
+            const int lead = __ffs(dm) - 1;
+            unsigned at = 0;
+            if (lane == lead) at = atomicAdd(&A.ctl->defer_n, (unsigned)__popc(dm));
+            at = __shfl_sync(0xffffffffu, at, lead);
+            if (active && !fast) A.defer[at + __popc(dm & ((1u << lane) - 1u))] = i;
         }
         NbrOut L{A.nbr, 0, P.N, i};
         int n = 0;
@@ -360,48 +376,148 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
         }                                                                             \
         n = 0;                                                                        \
     } while (0)
-        // flattened walk of the window rows in the staged region.  A step
-        // that finds its row finished moves to the next row and tests that
-        // row's first candidate in the same step, so rows cost no steps of
-        // their own (only empty rows do).  la = region cell of the row's
-        // first cell; rows advance by RX, planes by RX * RY.  The warp votes
-        // once per 8 steps, so queues drain at DLIST - 8.
-        bool done = !fast;
-        int la = (zlo * G::RY + ly - STENCIL) * G::RX + lx - STENCIL;
-        const int la_end = la + (zhi - zlo + 1) * (G::RX * G::RY);
-        int cy = 0, k = 0, kend = 0;
-        if (!done) row_span(s_off, la, k, kend);
+        // flattened walk of the window rows in the staged region, branch
+        // free: every step advances a finished row (la = region cell of the
+        // row's first cell; rows step by RX, planes by RX * RY) and tests one
+        // candidate, with selects, so the lanes never diverge.  Lanes past
+        // their last row (la >= la_end) see empty rows.  The warp votes once
+        // per 8 steps, so queues drain at DLIST - 8.
+        int la = 0, la_end = 0, cy = 0, k = 0, kend = 0;
+        if (fast) {
+            la = (zlo * G::RY + ly - STENCIL) * G::RX + lx - STENCIL;
+            la_end = la + (zhi - zlo + 1) * (G::RX * G::RY);
+            row_span(s_off, la, k, kend);
+        }
         for (;;) {
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
-                if (!done) {
-                    if (k >= kend) {
-                        la += G::RX;
-                        if (++cy == 2 * STENCIL + 1) {
-                            cy = 0;
-                            la += G::RX * G::RY - (2 * STENCIL + 1) * G::RX;
-                        }
-                        if (la >= la_end) done = true;
-                        else row_span(s_off, la, k, kend);
-                    }
-                    if (k < kend) {
-                        const float4 pj = sp[k];
-                        if (r2_scaled(ci.x, ci.y, ci.z, pj.x, pj.y, pj.z) < 4.0f)
-                            s_list[(n++) * T + threadIdx.x] = (unsigned short)k;
-                        ++k;
-                    }
-                }
+                const bool adv = k >= kend;
+                int la2 = la + G::RX, cy2 = cy + 1;
+                const bool wrap = cy2 == 2 * STENCIL + 1;
+                la2 += wrap ? G::RX * G::RY - (2 * STENCIL + 1) * G::RX : 0;
+                cy2 = wrap ? 0 : cy2;
+                la = adv ? la2 : la;
+                cy = adv ? cy2 : cy;
+                const bool live = la < la_end;
+                const int lc = live ? la : 0;
+                const int k2 = s_off[lc], e2 = s_off[lc + 2 * STENCIL + 1];
+                k = adv ? k2 : k;
+                kend = adv ? (live ? e2 : k2) : kend;
+                const bool valid = k < kend;
+                const float4 pj = sp[valid ? k : 0];
+                if (valid && r2_scaled(ci.x, ci.y, ci.z, pj.x, pj.y, pj.z) < 4.0f)
+                    s_list[(n++) * T + threadIdx.x] = (unsigned short)k;
+                k += valid ? 1 : 0;
             }
             if (__any_sync(0xffffffffu, n > DLIST - 8)) ASPH_DRAIN();
-            if (__all_sync(0xffffffffu, done)) break;
+            if (__all_sync(0xffffffffu, la >= la_end)) break;
         }
         ASPH_DRAIN();
 #undef ASPH_DRAIN
-        if (active) {
-            if (fast) A.nbr_cnt[i] = L.n <= NBR_CAP ? L.n : -1;
-            else s = density_target_global(P, A, i, pi, rr);
+        if (active && fast) {
+            A.nbr_cnt[i] = L.n <= NBR_CAP ? L.n : -1;
             density_eos_epilogue(P, A.out, i, pi, s, rr, dt);
         }
+    }
+}
+
+// Deferred pass: one warp per queued target.  The lanes read the ranges of
+// the window's cells (c = dz * 25 + dy * 5 + dx, the reference's loop order)
+// and their prefix counts into shared memory, then test the candidates 32
+// at a time: candidate g lies in the last cell whose prefix is <= g.
+// Accepted neighbours are appended in candidate order by ballot, so the list
+// has the order of the reference's loop; the sums are reduced over the warp
+// in a fixed tree.
+constexpr int DEF_TPB = 256;
+constexpr int WIN_CELLS = (2 * STENCIL + 1) * (2 * STENCIL + 1) * (2 * STENCIL + 1);
+static_assert(WIN_CELLS <= 128, "a window's cells fit four per lane");
+
+__global__ __launch_bounds__(DEF_TPB) void k_density_deferred(const __grid_constant__ Phys P,
+                                                              const __grid_constant__ DArgs A) {
+    __shared__ int s_cs[DEF_TPB / 32][128];   // first table index of window cell c
+    __shared__ int s_cp[DEF_TPB / 32][128];   // candidates in the cells before c
+    DevCtl* ctl = A.ctl;
+    if (ctl->aborted) return;
+    const unsigned nq = A.defer ? ctl->defer_n : (unsigned)P.N;   // no queue: every target
+    const int lane = threadIdx.x & 31;
+    int* cs = s_cs[threadIdx.x >> 5];
+    int* cp = s_cp[threadIdx.x >> 5];
+    const float dt = ctl->dt;
+    const unsigned nwarps = (gridDim.x * DEF_TPB) >> 5;
+    for (unsigned t = (blockIdx.x * DEF_TPB + threadIdx.x) >> 5; t < nq; t += nwarps) {
+        const int i = A.defer ? A.defer[t] : (int)t;
+        const float4 pi = A.pos[i];
+        const int ix = cell_ix(pi.x, P.inv_dx, P.nx), iy = cell_ix(pi.y, P.inv_dy, P.ny);
+        const int iz = cell_ix(pi.z, P.inv_dz, P.nz);
+        const int z0 = max(iz - STENCIL, 0), z1 = min(iz + STENCIL, P.nz - 1);
+        const int ncell = (z1 - z0 + 1) * (2 * STENCIL + 1) * (2 * STENCIL + 1);
+        int total = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int c = u * 32 + lane;
+            int2 rg = make_int2(0, 0);
+            if (c < ncell) {
+                const int dz = c / 25, r = c - dz * 25, dy = r / 5, dx = r - dy * 5;
+                const int gy = wrapi(iy - STENCIL + dy, P.ny), gx = wrapi(ix - STENCIL + dx, P.nx);
+                rg = A.range[(size_t)((z0 + dz) * P.ny + gy) * P.nx + gx];
+            }
+            const int cnt = rg.y - rg.x;
+            int x = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            cs[c] = rg.x;
+            cp[c] = total + x - cnt;
+            total += __shfl_sync(0xffffffffu, x, 31);
+        }
+        __syncwarp();
+        if (total > ASPH_MAX_CANDIDATES) {   // same stop as the global walk's budget
+            if (lane == 0) stop_run(ctl, ASPH_ERR_DENSE);
+            return;
+        }
+        const float3 ci = to_cells(P, pi.x, pi.y, pi.z);
+        const FF rr = snd_eval(P.snd_rho, P.snd_n, pi.z);
+        DSum s{0.f, 0.f, 0.f};
+        int nb = 0;
+        for (int g0 = 0; g0 < total; g0 += 32) {
+            const int g = g0 + lane;
+            bool push = false;
+            int j = 0;
+            if (g < total) {
+                int lo = 0, hi = ncell - 1;   // cp[lo] <= g
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (cp[mid] <= g) lo = mid; else hi = mid - 1;
+                }
+                j = cs[lo] + (g - cp[lo]);
+                const float4 pj = A.pos[j];
+                const float3 cj = to_cells(P, pj.x, pj.y, pj.z);
+                const float r2 = r2_scaled(ci.x, ci.y, ci.z, cj.x, cj.y, cj.z);
+                if (r2 < 4.0f) {
+                    dsum_add(s, r2, pj.w, rr);
+                    push = r2 >= 1e-12f;
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, push);
+            if (push) {
+                const int n = nb + __popc(m & ((1u << lane) - 1u));
+                if (n < NBR_CAP) A.nbr[(size_t)n * P.N + i] = j;
+            }
+            nb += __popc(m);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s.S1 += __shfl_xor_sync(0xffffffffu, s.S1, o);
+            s.S2 += __shfl_xor_sync(0xffffffffu, s.S2, o);
+            s.T += __shfl_xor_sync(0xffffffffu, s.T, o);
+        }
+        if (lane == 0) {
+            A.nbr_cnt[i] = nb <= NBR_CAP ? nb : -1;
+            density_eos_epilogue(P, A.out, i, pi, s, rr, dt);
+        }
+        __syncwarp();   // cs and cp are rewritten for the next target
     }
 }
 
@@ -544,14 +660,19 @@ constexpr Shape SHAPES[] = {{8, 8, 8}, {8, 8, 4}, {8, 4, 4}, {4, 4, 4}};
 constexpr int MAX_STAGE = 4096;      // staged particles per brick at most
 constexpr double STAGE_MARGIN = 1.35;
 
-int region_cells(const Shape& s) { return (s.bx + 2 * HALO) * (s.by + 2 * HALO) * (s.bz + 2 * HALO); }
+int region_cells(const Shape& s, int h) { return (s.bx + 2 * h) * (s.by + 2 * h) * (s.bz + 2 * h); }
+
+// Staged halo: with a sort every step the targets are in (or next to) the
+// cells of their brick, and the stencil alone is staged; slower cadences
+// stage one more cell of drift.  Targets outside either go to the deferred pass.
+int halo_for(const Phys& P) { return P.sort_every == 1 ? STENCIL : MAX_HALO; }
 
 // Largest brick whose region fits the grid without wrapping onto itself
 // and whose expected staged count (with a margin) fits the cap.
 bool fits(const Phys& P, int k) {
     const Shape& s = SHAPES[k];
-    if (P.nx < s.bx + 2 * HALO || P.ny < s.by + 2 * HALO) return false;
-    return region_cells(s) * ((double)P.N / (double)P.ncell) * STAGE_MARGIN <= MAX_STAGE;
+    if (P.nx < s.bx + 2 * MAX_HALO || P.ny < s.by + 2 * MAX_HALO) return false;
+    return region_cells(s, MAX_HALO) * ((double)P.N / (double)P.ncell) * STAGE_MARGIN <= MAX_STAGE;
 }
 
 int pick_shape(const Phys& P) {
@@ -571,14 +692,14 @@ struct Launch {
     size_t smem;
 };
 
-Launch plan(const Phys& P, const Shape& s) {
+Launch plan(const Phys& P, const Shape& s, int h) {
     Launch L;
     L.C.nbx = (P.nx + s.bx - 1) / s.bx;
     L.C.nby = (P.ny + s.by - 1) / s.by;
     L.C.nbz = (P.nz + s.bz - 1) / s.bz;
     L.C.nbricks = L.C.nbx * L.C.nby * L.C.nbz;
     const double ppc = (double)P.N / (double)P.ncell;
-    const int R = region_cells(s);
+    const int R = region_cells(s, h);
     int cap = (int)(R * ppc * STAGE_MARGIN) + 64;
     cap = (cap + 63) & ~63;
     L.C.cap = cap > MAX_STAGE ? MAX_STAGE : cap;
@@ -593,13 +714,32 @@ Launch plan(const Phys& P, const Shape& s) {
     return L;
 }
 
-template <int BX, int BY, int BZ>
-void launch_d(const Phys& P, const DArgs& A, cudaStream_t s) {
-    const Launch L = plan(P, Shape{BX, BY, BZ});
+// Blocks of the deferred pass: 4 per SM (32 warps), each warp looping over the queue.
+int deferred_blocks() {
+    static int blocks = 0;
+    if (!blocks) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+        blocks = 4 * sms;
+    }
+    return blocks;
+}
+
+template <int BX, int BY, int BZ, int H>
+void launch_dh(const Phys& P, const DArgs& A, cudaStream_t s) {
+    const Launch L = plan(P, Shape{BX, BY, BZ}, H);
     k_brick_spans<BX, BY, BZ><<<(L.C.nbricks + 255) / 256, 256, 0, s>>>(P, A.skeys, const_cast<int2*>(A.spans), L.C,
                                                                         A.ctl);
-    cudaFuncSetAttribute(k_density_brick<BX, BY, BZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
-    k_density_brick<BX, BY, BZ><<<L.C.nbricks, L.threads, L.smem, s>>>(P, A, L.C);
+    cudaFuncSetAttribute(k_density_brick<BX, BY, BZ, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+    k_density_brick<BX, BY, BZ, H><<<L.C.nbricks, L.threads, L.smem, s>>>(P, A, L.C);
+    k_density_deferred<<<deferred_blocks(), DEF_TPB, 0, s>>>(P, A);
+}
+
+template <int BX, int BY, int BZ>
+void launch_d(const Phys& P, const DArgs& A, cudaStream_t s) {
+    if (halo_for(P) == STENCIL) launch_dh<BX, BY, BZ, STENCIL>(P, A, s);
+    else launch_dh<BX, BY, BZ, MAX_HALO>(P, A, s);
 }
 
 inline int blocks_for(int n, int tpb) { return n <= 0 ? 1 : (n + tpb - 1) / tpb; }
@@ -631,7 +771,13 @@ void launch_density(const Phys& P, const Bufs& B, cudaStream_t s) {
     A.spans = B.spans;
     A.nbr = B.nbr;
     A.nbr_cnt = B.nbr_cnt;
+    A.defer = B.defer;
     A.ctl = B.ctl;
+    if (B.force_global == 2) {   // warp per target for every target
+        A.defer = nullptr;
+        k_density_deferred<<<deferred_blocks(), DEF_TPB, 0, s>>>(P, A);
+        return;
+    }
     switch (shape_in_use(P, B)) {
         case 0: launch_d<8, 8, 8>(P, A, s); break;
         case 1: launch_d<8, 8, 4>(P, A, s); break;

@@ -172,14 +172,14 @@ def _stages(p, s, simt=1500.0, global_path=False, tol=None):
 
 
 @pytest.mark.parametrize("name", ["ref_jitter", "ref_cluster", "ref_fast", "cfg_jitter", "cfg_uniform", "cfg_wide"])
-@pytest.mark.parametrize("path", ["brick", "global"])
+@pytest.mark.parametrize("path", ["brick", "global", "warp"])
 def test_stages_match_oracle(name, path):
     # ref_fast moves particles by more than a cell (250-500 m/s, far outside
     # the CFL envelope) to exercise the staged-region fallback; there the
     # viscous heating -v.a_visc/(c_p Pi) is a cancellation of O(100) K/s
     # terms clamped at 1 K/s, resolved by FP32 to ~1e-5 of the cap.
     tol = {"dthdt": 1e-4} if name == "ref_fast" else None
-    _stages(*_case(name), global_path=(path == "global"), tol=tol)
+    _stages(*_case(name), global_path={"brick": 0, "global": 1, "warp": 2}[path], tol=tol)
 
 
 # ---------------------------------------------------------------------------
@@ -397,10 +397,11 @@ def _lists_after_density(p, s, global_path):
     st = sim.get_state(("x", "y", "z"))
     cr = sim.get_sort()["cell_range"]
     sim.density_eos()
+    deferred = sim.control()["deferred"]
     cnt, lst = sim.neighbours()
     sim.close()
     sets = [np.sort(lst[:c, i]) for i, c in enumerate(cnt)]
-    return st, cr, cnt, sets
+    return st, cr, cnt, sets, lst, deferred
 
 
 def _window_rule(p, st, cr, i):
@@ -428,12 +429,20 @@ def _window_rule(p, st, cr, i):
 @pytest.mark.parametrize("name", ["cfg_jitter", "ref_fast", "cfg_wide"])
 def test_neighbour_lists_exact(name):
     p, s = _case(name)
-    st_b, cr, cnt_b, sets_b = _lists_after_density(p, s, False)
-    st_g, _, cnt_g, sets_g = _lists_after_density(p, s, True)
-    assert np.array_equal(st_b["x"], st_g["x"])
-    assert np.array_equal(cnt_b, cnt_g)
+    st_b, cr, cnt_b, sets_b, lst_b, deferred = _lists_after_density(p, s, 0)
+    st_g, _, cnt_g, sets_g, lst_g, _ = _lists_after_density(p, s, 1)
+    st_w, _, cnt_w, _, lst_w, _ = _lists_after_density(p, s, 2)
+    assert np.array_equal(st_b["x"], st_g["x"]) and np.array_equal(st_w["x"], st_g["x"])
+    assert np.array_equal(cnt_b, cnt_g) and np.array_equal(cnt_w, cnt_g)
     for i in range(p.n_particles):
         assert np.array_equal(sets_b[i], sets_g[i]), i
+    # all three paths list each target's neighbours in the reference's loop order
+    n = np.where(cnt_g < 0, 0, cnt_g)
+    slot = np.arange(lst_g.shape[0])[:, None] < n[None, :]
+    assert np.array_equal(np.where(slot, lst_b, -1), np.where(slot, lst_g, -1))
+    assert np.array_equal(np.where(slot, lst_w, -1), np.where(slot, lst_g, -1))
+    if name == "ref_fast":   # moved by more than a cell: the brick pass deferred some targets
+        assert deferred > 0
     # the window rule in float32 on a sample of targets
     rng = np.random.default_rng(0)
     for i in rng.choice(p.n_particles, size=min(300, p.n_particles), replace=False):
