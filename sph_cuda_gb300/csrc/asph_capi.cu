@@ -330,7 +330,7 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     AL(B.status, (size_t)B.npasses * B.ntiles * 256 * 8);
     AL(B.range, C * 8); AL(B.surf, N); AL(B.rain_delta, C * 4); AL(B.precip, (size_t)P.nxy * 4);
     AL(B.ctl, sizeof(DevCtl));
-    AL(B.spans, (size_t)pair_max_bricks(P) * 8);
+    AL(B.spans, pair_span_slots(P) * 8);
     AL(B.nbr, (size_t)NBR_CAP * N * 4);
     AL(B.nbr_cnt, N * 4);
     AL(B.defer, N * 4);
@@ -419,6 +419,7 @@ extern "C" int asph_set_option(asph_ctx* c, int option, int value) {
     }
     for (auto& g : c->gexec)   // captured graphs hold the old kernels and parameters
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    if (option != ASPH_OPT_SORT_EVERY) c->spans_valid = false;   // spans are per brick shape
     return ASPH_OK;
 }
 
@@ -506,6 +507,7 @@ static void do_sort_build(asph_ctx* c, int force) {
     launch_sort(c->P, c->B, force, c->stream);
     launch_gather(c->P, c->B, G_SORTED | (force ? G_FORCE : 0), c->stream);
     c->B.pc ^= 1; c->B.vc ^= 1; c->B.qc ^= 1;
+    if (force) c->spans_valid = true;   // the gather of a sort writes the brick spans
     // source-term tendencies follow their particles (a step keeps them in its momentum pass)
     if (c->B.src)
         cudaMemcpyAsync(c->B.src, c->B.src_tmp, (size_t)c->P.N * 16, cudaMemcpyDeviceToDevice, c->stream);
@@ -715,7 +717,7 @@ extern "C" int asph_get_control(asph_ctx* c, AsphControl* o) {
     o->umax = h.umax; o->vmax = h.vmax; o->wmax = h.wmax;
     o->step = h.step; o->trips = h.trips; o->sort_count = h.sort_count; o->aborted = h.aborted;
     o->clamp_pending = h.clamp_pending; o->do_sort = h.do_sort; o->error = h.error; o->surf_count = h.surf_count;
-    o->deferred = (int32_t)h.defer_n;
+    o->deferred = (int32_t)h.defer_last;
     return ASPH_OK;
 }
 
@@ -815,8 +817,15 @@ extern "C" int asph_kick_drift_flux(asph_ctx* c) {
     return sync_status(c);
 }
 
+void asph::ensure_spans(asph_ctx* c) {
+    if (c->spans_valid) return;
+    launch_brick_spans(c->P, c->B, c->stream);
+    c->spans_valid = true;
+}
+
 extern "C" int asph_density_eos(asph_ctx* c) {
     if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
+    ensure_spans(c);
     launch_density(c->P, c->B, c->stream);
     c->lists_valid = true;
     CKR(cudaGetLastError());
@@ -863,6 +872,7 @@ void asph::enqueue_step(asph_ctx* c) {
 extern "C" int asph_step_profiled(asph_ctx* c, int nsteps, float* phase_ms) {
     if (!c || !phase_ms) return fail(ASPH_ERR_ARG, "NULL argument");
     if (!c->initialised) return fail(ASPH_ERR_STATE, "step before init/set_state");
+    ensure_spans(c);
     const Phys& P = c->P;
     cudaEvent_t ev[7];
     for (auto& e : ev) CKR(cudaEventCreate(&e));
@@ -943,6 +953,7 @@ extern "C" int asph_step_kernels(asph_ctx* c, int* n) {
 extern "C" int asph_step_async(asph_ctx* c, int nsteps) {
     if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
     if (!c->initialised) return fail(ASPH_ERR_STATE, "step before init/set_state");
+    ensure_spans(c);
     for (int k = 0; k < nsteps; ++k) {
         const int slot = graph_slot(c->B);
         if (!c->gexec[slot]) {

@@ -16,6 +16,7 @@ struct asph_ctx {
     bool own_stream = false;
     bool initialised = false;
     bool lists_valid = false;   // neighbour lists match the current positions
+    bool spans_valid = false;   // brick spans match the sorted keys and the brick shape in use
     // graphs keyed by the ping-pong state at the start of the step
     cudaGraphExec_t gexec[16] = {};
     int graph_kernels = 0;      // kernel nodes of a captured step graph
@@ -72,6 +73,9 @@ int graph_slot(const Bufs& B);
 void apply_pending_clamp(asph_ctx* c);
 bool reads_rain(const Phys& P);
 int reset_control(asph_ctx* c);
+// Recompute the brick spans from the sorted keys when no sort's gather wrote
+// them for the current keys and brick shape (outside any graph capture).
+void ensure_spans(asph_ctx* c);
 }  // namespace asph
 
 #define CKR(x)                                                                                  \

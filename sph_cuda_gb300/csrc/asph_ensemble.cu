@@ -133,6 +133,7 @@ extern "C" int asph_snapshot_restore(asph_ctx* c, const asph_snapshot* s) {
     CKR(cudaMemcpyAsync(c->B.ctl, s->ctl, offsetof(DevCtl, epoch), cudaMemcpyDeviceToDevice, c->stream));
     c->initialised = true;
     c->lists_valid = false;
+    c->spans_valid = false;   // the restored sorted keys' brick spans are rebuilt before the next pass
     return ASPH_OK;
 }
 
@@ -361,6 +362,7 @@ extern "C" int asph_ens_step_async(asph_ens* e, int nsteps) {
     if (!e) return fail(ASPH_ERR_ARG, "NULL argument");
     for (asph_ctx* c : e->m)
         if (!c->initialised) return fail(ASPH_ERR_STATE, "ensemble step before init");
+    for (asph_ctx* c : e->m) ensure_spans(c);   // on each member's stream, before the origin waits on it
     int st = origin_after_members(e);
     if (st) return st;
     std::vector<int> key(e->m.size());

@@ -26,6 +26,8 @@ struct DevCtl {
     int step, trips, sort_count, aborted, clamp_pending, do_sort, error, surf_count;
     int sorted_this_step;
     unsigned defer_n;          // targets queued for the density pass's deferred kernel
+    unsigned defer_done;       // finished blocks of the deferred kernel (the last resets defer_n)
+    unsigned defer_last;       // targets the last density pass deferred
     unsigned gmax[3];          // float bits of |u|,|v|,|w| maxima (atomicMax)
     unsigned done;             // finished-block counter of the momentum pass
     unsigned epoch;            // radix look-back epoch
@@ -68,7 +70,8 @@ struct Bufs {
     float*  precip;     // accumulated surface precipitation [kg/m^2]
     DevCtl* ctl;
     float4* snd;        // sounding tables: rho_ref, pres_ref, thvr (3 x snd_n nodes)
-    int2*   spans;      // per brick of the density pass: its span of targets in the sorted order
+    int2*   spans;      // per brick of the density pass, by the brick's Morton id (its keys >> log2 of the
+                        // brick's key count): its span of targets in the sorted order, {0,0} when empty
     int*    nbr;        // neighbour lists of the density pass, slot-major [NBR_CAP][N]
     int*    nbr_cnt;    // neighbours per particle, -1 when the list overflowed
     int*    defer;      // targets of the density pass left to its deferred kernel (N slots)
@@ -112,8 +115,14 @@ void launch_rain(const Phys& P, const Bufs& B, cudaStream_t s);
 // Brick shape index the density pass uses (-1: per-target global path),
 // the number of shapes, and whether shape k suits the grid and density.
 int pair_shape(const Phys& P, const Bufs& B);
-// Most bricks any brick shape needs for this grid (sizes Bufs::spans).
-int pair_max_bricks(const Phys& P);
+// Entries of Bufs::spans: Morton ids of the smallest brick shape.
+size_t pair_span_slots(const Phys& P);
+// log2 of the key count of the brick shape in use (its spans are indexed by
+// key >> shift), -1 on the global path.
+int pair_span_shift(const Phys& P, const Bufs& B);
+// Every brick's span by binary search in the sorted keys: for spans that the
+// last sort's gather did not write (restored sorted keys, another brick shape).
+void launch_brick_spans(const Phys& P, const Bufs& B, cudaStream_t s);
 int pair_shape_count();
 bool pair_shape_fits(const Phys& P, int k);
 void launch_cfl(const Phys& P, const Bufs& B, cudaStream_t s);

@@ -86,6 +86,8 @@ struct GArgs {
     const float4* acc;
     const uint32_t *perm, *skeys;
     int2* range;
+    int2* spans;         // brick spans of the density pass by Morton id (NULL: global path) ...
+    int span_shift;      // ... a brick's id is its keys >> span_shift
     uint8_t* surf;
     uint32_t* kin;
     const float4* src;   // source-term tendencies (NULL: hook off) ...
@@ -132,6 +134,19 @@ __global__ __launch_bounds__(TPB) void k_gather(const __grid_constant__ Phys P, 
                 }
             }
             if (i == P.N - 1 && cin) A.range[c].y = P.N;
+            if (A.spans) {   // the same boundaries at brick granularity
+                const uint32_t bc = kc >> A.span_shift;
+                if (i == 0) {
+                    A.spans[bc].x = 0;
+                } else {
+                    const uint32_t bp = A.skeys[i - 1] >> A.span_shift;
+                    if (bc != bp) {
+                        A.spans[bc].x = i;
+                        A.spans[bp].y = i;
+                    }
+                }
+                if (i == P.N - 1) A.spans[bc].y = P.N;
+            }
             surf = ((int)__fmul_rn(p.z, P.inv_dz)) == 0;
             A.surf[i] = surf ? 1 : 0;
             const unsigned m = __ballot_sync(__activemask(), surf);
@@ -337,6 +352,8 @@ void launch_gather(const Phys& P, const Bufs& B, int mode, cudaStream_t s) {
     A.pos_src = B.pos[B.pc]; A.vel_src = B.vel[B.vc]; A.thq_src = B.thq[B.qc];
     A.pos_dst = B.pos[1 - B.pc]; A.vel_dst = B.vel[1 - B.vc]; A.thq_dst = B.thq[1 - B.qc];
     A.rp = B.rp; A.acc = B.acc; A.perm = B.perm; A.skeys = B.skeys; A.range = B.range;
+    A.span_shift = pair_span_shift(P, B);
+    A.spans = A.span_shift >= 0 ? B.spans : nullptr;
     A.surf = B.surf; A.kin = B.kin; A.ctl = B.ctl;
     A.src = B.src; A.src_tmp = B.src_tmp;
     k_gather<<<blocks_for(P.N), TPB, 0, s>>>(P, A, mode);

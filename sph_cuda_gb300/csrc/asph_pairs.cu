@@ -52,6 +52,8 @@ struct BrickGeom {
     static constexpr int RX = BX + 2 * H, RY = BY + 2 * H, RZ = BZ + 2 * H;
     static constexpr int R = RX * RY * RZ;
     static constexpr int KEYS = BX * BY * BZ;
+    static constexpr int LOG2K = KEYS == 512 ? 9 : KEYS == 256 ? 8 : KEYS == 128 ? 7 : 6;
+    static_assert((1 << LOG2K) == KEYS, "brick key count is a power of two");
 };
 
 struct PairCfg {
@@ -238,17 +240,19 @@ struct DArgs {
 
 // Every brick's span of targets in the sorted order: the brick is a
 // Morton-aligned key range, found by binary search in the sorted keys (one
-// thread per brick, before the pass, so that no CTA of the pass waits on it).
+// thread per brick).  The gather writes the same spans when a sort runs; this
+// kernel serves sorted keys that the gather did not see (a restored state,
+// another brick shape).
 template <int BX, int BY, int BZ>
 __global__ void k_brick_spans(const __grid_constant__ Phys P, const uint32_t* __restrict__ skeys, int2* spans,
-                              PairCfg C, DevCtl* ctl) {
+                              PairCfg C) {
     using G = BrickGeom<BX, BY, BZ, STENCIL>;
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b == 0) ctl->defer_n = 0;   // the deferred queue of the pass that follows
-    if (b >= C.nbricks || ctl->aborted) return;
+    if (b >= C.nbricks) return;
     const int bxi = b % C.nbx, byi = (b / C.nbx) % C.nby, bzi = b / (C.nbx * C.nby);
     const uint32_t base = morton3((uint32_t)(bxi * BX), (uint32_t)(byi * BY), (uint32_t)(bzi * BZ));
-    spans[b] = make_int2(lower_bound_u32(skeys, P.N, base), lower_bound_u32(skeys, P.N, base + (uint32_t)G::KEYS));
+    spans[base >> G::LOG2K] =
+        make_int2(lower_bound_u32(skeys, P.N, base), lower_bound_u32(skeys, P.N, base + (uint32_t)G::KEYS));
 }
 
 __device__ __forceinline__ DSum density_target_global(const Phys& P, const DArgs& A, int i, float4 pi, FF rr) {
@@ -292,11 +296,15 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
     unsigned short* s_list = reinterpret_cast<unsigned short*>(s_start);      // DLIST x T
     __shared__ int s_warp[32];
     __shared__ int s_span[2];
-    if (A.ctl->aborted) return;
+    __shared__ int s_run;
+    if (threadIdx.x == 0) s_run = A.ctl->aborted ? 0 : 1;   // one decision per block (barriers follow)
+    __syncthreads();
+    if (!s_run) return;
     const int b = blockIdx.x;
     const int bxi = b % C.nbx, byi = (b / C.nbx) % C.nby, bzi = b / (C.nbx * C.nby);
     if (threadIdx.x == 0) {
-        const int2 sp2 = A.spans[b];
+        const int2 sp2 =
+            A.spans[morton3((uint32_t)(bxi * BX), (uint32_t)(byi * BY), (uint32_t)(bzi * BZ)) >> G::LOG2K];
         s_span[0] = sp2.x;
         s_span[1] = sp2.y;
     }
@@ -436,9 +444,11 @@ __global__ __launch_bounds__(DEF_TPB) void k_density_deferred(const __grid_const
                                                               const __grid_constant__ DArgs A) {
     __shared__ int s_cs[DEF_TPB / 32][128];   // first table index of window cell c
     __shared__ int s_cp[DEF_TPB / 32][128];   // candidates in the cells before c
+    __shared__ int s_run;
     DevCtl* ctl = A.ctl;
-    if (ctl->aborted) return;
-    const unsigned nq = A.defer ? ctl->defer_n : (unsigned)P.N;   // no queue: every target
+    if (threadIdx.x == 0) s_run = ctl->aborted ? 0 : 1;   // one decision per block: every thread
+    __syncthreads();                                       // reaches the barrier at the end
+    const unsigned nq = !s_run ? 0u : (A.defer ? ctl->defer_n : (unsigned)P.N);   // no queue: every target
     const int lane = threadIdx.x & 31;
     int* cs = s_cs[threadIdx.x >> 5];
     int* cp = s_cp[threadIdx.x >> 5];
@@ -473,9 +483,9 @@ __global__ __launch_bounds__(DEF_TPB) void k_density_deferred(const __grid_const
             total += __shfl_sync(0xffffffffu, x, 31);
         }
         __syncwarp();
-        if (total > ASPH_MAX_CANDIDATES) {   // same stop as the global walk's budget
+        if (total > ASPH_MAX_CANDIDATES) {   // same stop as the global walk's budget (total is warp-uniform)
             if (lane == 0) stop_run(ctl, ASPH_ERR_DENSE);
-            return;
+            break;
         }
         const float3 ci = to_cells(P, pi.x, pi.y, pi.z);
         const FF rr = snd_eval(P.snd_rho, P.snd_n, pi.z);
@@ -518,6 +528,17 @@ __global__ __launch_bounds__(DEF_TPB) void k_density_deferred(const __grid_const
             density_eos_epilogue(P, A.out, i, pi, s, rr, dt);
         }
         __syncwarp();   // cs and cp are rewritten for the next target
+    }
+    if (A.defer) {   // the last block to finish empties the queue for the next pass
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(&ctl->defer_done, 1u) == gridDim.x - 1) {
+                ctl->defer_last = ctl->defer_n;
+                ctl->defer_n = 0u;
+                ctl->defer_done = 0u;
+            }
+        }
     }
 }
 
@@ -729,8 +750,6 @@ int deferred_blocks() {
 template <int BX, int BY, int BZ, int H>
 void launch_dh(const Phys& P, const DArgs& A, cudaStream_t s) {
     const Launch L = plan(P, Shape{BX, BY, BZ}, H);
-    k_brick_spans<BX, BY, BZ><<<(L.C.nbricks + 255) / 256, 256, 0, s>>>(P, A.skeys, const_cast<int2*>(A.spans), L.C,
-                                                                        A.ctl);
     cudaFuncSetAttribute(k_density_brick<BX, BY, BZ, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
     k_density_brick<BX, BY, BZ, H><<<L.C.nbricks, L.threads, L.smem, s>>>(P, A, L.C);
     k_density_deferred<<<deferred_blocks(), DEF_TPB, 0, s>>>(P, A);
@@ -747,13 +766,30 @@ inline int blocks_for(int n, int tpb) { return n <= 0 ? 1 : (n + tpb - 1) / tpb;
 }  // namespace
 
 int pair_shape(const Phys& P, const Bufs& B) { return shape_in_use(P, B); }
-int pair_max_bricks(const Phys& P) {
-    int m = 1;
-    for (const Shape& sh : SHAPES) {
-        const int n = ((P.nx + sh.bx - 1) / sh.bx) * ((P.ny + sh.by - 1) / sh.by) * ((P.nz + sh.bz - 1) / sh.bz);
-        m = n > m ? n : m;
+size_t pair_span_slots(const Phys& P) {
+    const size_t keys = (size_t)1 << P.key_bits;
+    return keys >> 6 > 0 ? keys >> 6 : 1;   // the smallest shape, 4 x 4 x 4, has 64 keys
+}
+int pair_span_shift(const Phys& P, const Bufs& B) {
+    const int k = shape_in_use(P, B);
+    if (k < 0) return -1;
+    const int keys = SHAPES[k].bx * SHAPES[k].by * SHAPES[k].bz;
+    int sh = 0;
+    while ((1 << sh) < keys) ++sh;
+    return sh;
+}
+void launch_brick_spans(const Phys& P, const Bufs& B, cudaStream_t s) {
+    const int k = shape_in_use(P, B);
+    if (k < 0) return;
+    const Shape& sh = SHAPES[k];
+    const Launch L = plan(P, sh, MAX_HALO);
+    const int blocks = (L.C.nbricks + 255) / 256;
+    switch (k) {
+        case 0: k_brick_spans<8, 8, 8><<<blocks, 256, 0, s>>>(P, B.skeys, B.spans, L.C); break;
+        case 1: k_brick_spans<8, 8, 4><<<blocks, 256, 0, s>>>(P, B.skeys, B.spans, L.C); break;
+        case 2: k_brick_spans<8, 4, 4><<<blocks, 256, 0, s>>>(P, B.skeys, B.spans, L.C); break;
+        default: k_brick_spans<4, 4, 4><<<blocks, 256, 0, s>>>(P, B.skeys, B.spans, L.C); break;
     }
-    return m;
 }
 int pair_shape_count() { return (int)(sizeof(SHAPES) / sizeof(SHAPES[0])); }
 bool pair_shape_fits(const Phys& P, int k) { return k >= 0 && k < pair_shape_count() && fits(P, k); }

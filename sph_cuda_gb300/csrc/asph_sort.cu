@@ -79,8 +79,8 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp
 // Clears the cell table before it is rebuilt (the reference's
 // cudaMemsetAsync(cellRange), asph_h100.cu:971-972), resets the sort
 // counters, and zeroes this step's rain deposits.
-__global__ void k_sort_prep(Phys P, int2* __restrict__ range, float* __restrict__ delta,
-                            DevCtl* __restrict__ ctl, int force, int clear_delta) {
+__global__ void k_sort_prep(Phys P, int2* __restrict__ range, int2* __restrict__ spans, int nspans,
+                            float* __restrict__ delta, DevCtl* __restrict__ ctl, int force, int clear_delta) {
     const bool run = sort_runs(ctl, force);
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -105,6 +105,7 @@ __global__ void k_sort_prep(Phys P, int2* __restrict__ range, float* __restrict_
     const int n4 = P.ncell >> 1;
     for (int i = t0; i < n4; i += stride) r4[i] = make_int4(0, 0, 0, 0);
     if ((P.ncell & 1) && t0 == 0) range[P.ncell - 1] = make_int2(0, 0);
+    for (int i = t0; i < nspans; i += stride) spans[i] = make_int2(0, 0);   // brick spans, rebuilt with the table
 }
 
 // Digit histograms of every pass in one read of the keys.
@@ -429,7 +430,9 @@ void sort_inc_sizes(int N, int* max_keys, int* tiles, int* blocks) {
 void launch_sort_prep(const Phys& P, const Bufs& B, int force, int clear_delta, cudaStream_t s) {
     int blocks = (P.ncell / 2 + TPB - 1) / TPB;
     blocks = blocks < 1 ? 1 : (blocks > 152 * 16 ? 152 * 16 : blocks);
-    k_sort_prep<<<blocks, TPB, 0, s>>>(P, B.range, B.rain_delta, B.ctl, force, clear_delta);
+    const int shift = pair_span_shift(P, B);
+    const int nspans = shift >= 0 ? (int)(((size_t)1 << P.key_bits) >> shift) : 0;
+    k_sort_prep<<<blocks, TPB, 0, s>>>(P, B.range, B.spans, nspans, B.rain_delta, B.ctl, force, clear_delta);
 }
 
 void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s) {

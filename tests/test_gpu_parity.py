@@ -505,3 +505,34 @@ def test_step_sort_is_the_stable_sort_of_its_keys(speed, shuffle):
     if not shuffle and speed < 10:
         assert 0 < max(changed) < p.n_particles // 8    # the incremental path ran
     sim.close()
+
+
+# ---------------------------------------------------------------------------
+# brick spans: written by the gather of each sort, rebuilt from the sorted
+# keys after a brick-shape change or a restore between sorts
+# ---------------------------------------------------------------------------
+def test_brick_spans_follow_shape_changes_and_restores():
+    p = small_config(lat=(32, 32, 32), grid=(40, 40, 80), sort_every=0)   # sorts gated by displacement
+    a = Asph(p)
+    a.init()
+    a.step(2)
+    snap = a.snapshot()
+    a.step(1)
+    ref = a.get_state()
+    ref_cnt, ref_lst = a.neighbours()
+    for shape in (1, 2, 3, 0):
+        a.restore(snap)
+        a.set_pair_shape(shape)
+        a.step(1)
+        got = a.get_state()
+        cnt, lst = a.neighbours()
+        # every target was processed once, by its brick or by the deferred pass
+        assert np.array_equal(cnt, ref_cnt), shape
+        for k in ("x", "y", "z", "u", "v", "w", "th", "qv", "qc", "rho", "prs"):
+            assert normwise(got[k], ref[k]) < 1e-6, (shape, k, normwise(got[k], ref[k]))
+        n = np.where(ref_cnt < 0, 0, ref_cnt)
+        slot = np.arange(lst.shape[0])[:, None] < n[None, :]
+        assert np.array_equal(np.where(slot, lst, -1), np.where(slot, ref_lst, -1)), shape
+        # the pass found nearly every target in its brick
+        assert a.control()["deferred"] < p.n_particles // 20, (shape, a.control()["deferred"])
+    a.close()
