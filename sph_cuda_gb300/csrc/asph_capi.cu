@@ -326,7 +326,7 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
         AL(B.pos[k], N * 16); AL(B.vel[k], N * 16); AL(B.thq[k], N * 16);
         AL(B.kbuf[k], N * 4); AL(B.vbuf[k], N * 4); AL(B.rain[k], C * 4);
     }
-    AL(B.rp, N * 8); AL(B.acc, N * 16); AL(B.dthdt, N * 4); AL(B.kin, N * 4);
+    AL(B.rp, N * 8); AL(B.acc, N * 16); AL(B.ms[0], N * 16); AL(B.ms[1], N * 16); AL(B.dthdt, N * 4); AL(B.kin, N * 4);
     AL(B.status, (size_t)B.npasses * B.ntiles * 256 * 8);
     AL(B.range, C * 8); AL(B.surf, N); AL(B.rain_delta, C * 4); AL(B.precip, (size_t)P.nxy * 4);
     AL(B.ctl, sizeof(DevCtl));

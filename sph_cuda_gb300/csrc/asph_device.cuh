@@ -154,6 +154,9 @@ struct DOut {
     float2* rp;
     const float* rain_cur;
     float* rain_dep;
+    const float4* vel;   // velocities the momentum pass reads (after the first half kick) ...
+    float4* ms0;         // ... packed for its neighbour loads: x, y, z, p' ...
+    float4* ms1;         // ... and u, v, w, rho
 };
 __device__ __forceinline__ void density_eos_epilogue(const Phys& P, const DOut& O, int i, float4 pi, const DSum& s,
                                                      const FF& rr, float dt) {
@@ -235,6 +238,9 @@ __device__ __forceinline__ void density_eos_epilogue(const Phys& P, const DOut& 
     qc = fmaxf(qc, 0.0f);
     O.thq[i] = make_float4(th, qv, qc, t.w);
     O.rp[i] = make_float2(rho, ppr);
+    const float4 v = O.vel[i];
+    O.ms0[i] = make_float4(pi.x, pi.y, pi.z, ppr);
+    O.ms1[i] = make_float4(v.x, v.y, v.z, rho);
 }
 
 // Momentum pair accumulation (asph_h100.cu:448-492), arithmetic rearranged

@@ -47,6 +47,7 @@ struct Bufs {
     float4* vel[2];     // u, v, w, -
     float4* thq[2];     // theta, qv, qc, -
     float2* rp;         // rho_new, p'
+    float4* ms[2];      // written by the density pass for the momentum pass: (x, y, z, p'), (u, v, w, rho)
     float4* acc;        // ax, ay, az, -
     float*  dthdt;
     uint32_t* kin;      // keys of the current order (input of the next sort)

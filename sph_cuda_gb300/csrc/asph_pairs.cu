@@ -552,7 +552,9 @@ struct MArgs {
     const int2* range;
     const int* nbr;
     const int* nbr_cnt;
-    int use_lists;         // lists were produced on the current positions
+    int use_lists;         // lists (and ms0/ms1) were produced on the current positions and velocities
+    const float4* ms0;     // x, y, z, p' of the density pass
+    const float4* ms1;     // u, v, w, rho of the density pass
     MOut out;
     const float* rain_in;
     const float* rain_delta;
@@ -594,14 +596,24 @@ __global__ __launch_bounds__(M_TPB, 4) void k_momentum(const __grid_constant__ P
             if (aborted) {
                 if (mode & M_INTEGRATE) A.out.vel_out[i] = A.vel[i];
             } else {
-                const float4 p = A.pos[i], v = A.vel[i];
-                const float2 r = A.rp[i];
+                // (x, y, z, p') and (u, v, w, rho): packed by the density pass
+                // when the lists are current, else from the state buffers
+                float4 a, b;
+                if (A.use_lists) {
+                    a = A.ms0[i];
+                    b = A.ms1[i];
+                } else {
+                    const float4 p = A.pos[i], v = A.vel[i];
+                    const float2 r = A.rp[i];
+                    a = make_float4(p.x, p.y, p.z, r.y);
+                    b = make_float4(v.x, v.y, v.z, r.x);
+                }
                 MTarget T;
-                T.x = p.x; T.y = p.y; T.z = p.z;
-                T.u = v.x; T.v = v.y; T.w = v.z;
-                T.rhoi = fmaxf(r.x, 1e-3f);
+                T.x = a.x; T.y = a.y; T.z = a.z;
+                T.u = b.x; T.v = b.y; T.w = b.z;
+                T.rhoi = fmaxf(b.w, 1e-3f);
                 T.irhoi = __frcp_rn(T.rhoi);
-                T.pri = r.y;
+                T.pri = a.w;
                 MSum s{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 const int cnt = A.use_lists ? A.nbr_cnt[i] : -1;
                 if (cnt >= 0) {
@@ -610,26 +622,19 @@ __global__ __launch_bounds__(M_TPB, 4) void k_momentum(const __grid_constant__ P
                     for (; q + 4 <= cnt; q += 4) {
                         int jj[4];
                         float4 pp[4], vv[4];
-                        float2 rr[4];
 #pragma unroll
                         for (int u = 0; u < 4; ++u) jj[u] = A.nbr[(size_t)(q + u) * P.N + i];
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
-                            pp[u] = A.pos[jj[u]];
-                            rr[u] = A.rp[jj[u]];
-                            vv[u] = A.vel[jj[u]];
+                            pp[u] = A.ms0[jj[u]];
+                            vv[u] = A.ms1[jj[u]];
                         }
 #pragma unroll
-                        for (int u = 0; u < 4; ++u)
-                            msum_add(P, s, T, make_float4(pp[u].x, pp[u].y, pp[u].z, rr[u].y),
-                                     make_float4(vv[u].x, vv[u].y, vv[u].z, rr[u].x));
+                        for (int u = 0; u < 4; ++u) msum_add(P, s, T, pp[u], vv[u]);
                     }
                     for (; q < cnt; ++q) {
                         const int j = A.nbr[(size_t)q * P.N + i];
-                        const float4 pj = A.pos[j];
-                        const float2 rj = A.rp[j];
-                        const float4 vj = A.vel[j];
-                        msum_add(P, s, T, make_float4(pj.x, pj.y, pj.z, rj.y), make_float4(vj.x, vj.y, vj.z, rj.x));
+                        msum_add(P, s, T, A.ms0[j], A.ms1[j]);
                     }
                 } else {
                     s = momentum_target_global(P, A, T);
@@ -801,6 +806,9 @@ void launch_density(const Phys& P, const Bufs& B, cudaStream_t s) {
     A.skeys = B.skeys;
     A.out.thq = B.thq[B.qc];
     A.out.rp = B.rp;
+    A.out.vel = B.vel[B.vc];
+    A.out.ms0 = B.ms[0];
+    A.out.ms1 = B.ms[1];
     const bool reads = P.accretion || P.rain_evap;
     A.out.rain_cur = B.rain[B.rc];
     A.out.rain_dep = reads ? B.rain_delta : B.rain[B.rc];
@@ -832,6 +840,8 @@ void launch_momentum(const Phys& P, const Bufs& B, int mode, int use_lists, cuda
     A.nbr = B.nbr;
     A.nbr_cnt = B.nbr_cnt;
     A.use_lists = use_lists;
+    A.ms0 = B.ms[0];
+    A.ms1 = B.ms[1];
     A.out.thq = B.thq[B.qc];
     A.out.acc = B.acc;
     A.out.dthdt = B.dthdt;
