@@ -406,11 +406,14 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
                 cy2 = wrap ? 0 : cy2;
                 la = adv ? la2 : la;
                 cy = adv ? cy2 : cy;
-                const bool live = la < la_end;
-                const int lc = live ? la : 0;
-                const int k2 = s_off[lc], e2 = s_off[lc + 2 * STENCIL + 1];
-                k = adv ? k2 : k;
-                kend = adv ? (live ? e2 : k2) : kend;
+                if (adv) {   // predicated loads: only lanes that change rows read the offsets
+                    if (la < la_end) {
+                        k = s_off[la];
+                        kend = s_off[la + 2 * STENCIL + 1];
+                    } else {
+                        kend = k;
+                    }
+                }
                 const bool valid = k < kend;
                 const float4 pj = sp[valid ? k : 0];
                 if (valid && r2_scaled(ci.x, ci.y, ci.z, pj.x, pj.y, pj.z) < 4.0f)
@@ -462,15 +465,21 @@ __global__ __launch_bounds__(DEF_TPB) void k_density_deferred(const __grid_const
         const int z0 = max(iz - STENCIL, 0), z1 = min(iz + STENCIL, P.nz - 1);
         const int ncell = (z1 - z0 + 1) * (2 * STENCIL + 1) * (2 * STENCIL + 1);
         int total = 0;
+        int2 rgs[4];   // the four cell-range loads in flight together
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int c = u * 32 + lane;
-            int2 rg = make_int2(0, 0);
+            rgs[u] = make_int2(0, 0);
             if (c < ncell) {
                 const int dz = c / 25, r = c - dz * 25, dy = r / 5, dx = r - dy * 5;
                 const int gy = wrapi(iy - STENCIL + dy, P.ny), gx = wrapi(ix - STENCIL + dx, P.nx);
-                rg = A.range[(size_t)((z0 + dz) * P.ny + gy) * P.nx + gx];
+                rgs[u] = A.range[(size_t)((z0 + dz) * P.ny + gy) * P.nx + gx];
             }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int c = u * 32 + lane;
+            const int2 rg = rgs[u];
             const int cnt = rg.y - rg.x;
             int x = cnt;
 #pragma unroll
@@ -491,18 +500,31 @@ __global__ __launch_bounds__(DEF_TPB) void k_density_deferred(const __grid_const
         const FF rr = snd_eval(P.snd_rho, P.snd_n, pi.z);
         DSum s{0.f, 0.f, 0.f};
         int nb = 0;
-        for (int g0 = 0; g0 < total; g0 += 32) {
-            const int g = g0 + lane;
-            bool push = false;
-            int j = 0;
-            if (g < total) {
-                int lo = 0, hi = ncell - 1;   // cp[lo] <= g
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (cp[mid] <= g) lo = mid; else hi = mid - 1;
+        for (int g0 = 0; g0 < total; g0 += 64) {
+            // two rounds of 32 candidates: both rounds' loads in flight together
+            int jr[2];
+            float4 pr[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int g = g0 + 32 * h + lane;
+                jr[h] = 0;
+                if (g < total) {
+                    int lo = 0, hi = ncell - 1;   // cp[lo] <= g
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (cp[mid] <= g) lo = mid; else hi = mid - 1;
+                    }
+                    jr[h] = cs[lo] + (g - cp[lo]);
+                    pr[h] = A.pos[jr[h]];
                 }
-                j = cs[lo] + (g - cp[lo]);
-                const float4 pj = A.pos[j];
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+            const int g = g0 + 32 * h + lane;
+            bool push = false;
+            const int j = jr[h];
+            if (g < total) {
+                const float4 pj = pr[h];
                 const float3 cj = to_cells(P, pj.x, pj.y, pj.z);
                 const float r2 = r2_scaled(ci.x, ci.y, ci.z, cj.x, cj.y, cj.z);
                 if (r2 < 4.0f) {
@@ -516,6 +538,7 @@ __global__ __launch_bounds__(DEF_TPB) void k_density_deferred(const __grid_const
                 if (n < NBR_CAP) A.nbr[(size_t)n * P.N + i] = j;
             }
             nb += __popc(m);
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
