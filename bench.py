@@ -154,7 +154,13 @@ def oracle_initial_state(p):
 
 def workload_string(name: str) -> str:
     return {"bubble2m": "moist bubble, 2,097,152 particles, 133x133x200 cells, sort every step",
-            "bubble524k": "moist bubble, 524,288 particles, 66x66x200 cells, sort every step"}[name]
+            "bubble524k": "moist bubble, 524,288 particles, 66x66x200 cells, sort every step",
+            "reference128": "the reference's own geometry and init, 128x128x128 cells, dt 0.25 s, "
+                            "sort every step"}[name]
+
+
+def metric_for(p) -> str:
+    return "particle-steps/s (plain step, {:,} particles)".format(int(p.n_particles))
 
 
 def run_reference(args):
@@ -189,8 +195,15 @@ def run_reference(args):
 def workload_params(name: str):
     """bubble2m: the headline 2,097,152-particle moist-bubble workload.
     bubble524k: the same physics, cell size and density on a 10 x 10 x 8 km box
-    (64 x 64 x 128 lattice, 66 x 66 x 200 cells) for profiler captures."""
+    (64 x 64 x 128 lattice, 66 x 66 x 200 cells) for profiler captures.
+    reference128: the reference's own configuration at --nx --ny --nz 128 and
+    --dt 0.25 with a sort every step (what oracle/time_reference.py native runs)."""
     import sph_cuda_gb300 as sph
+    if name == "reference128":
+        p = sph.preset("reference", 128, 128, 128)
+        p.sort_every = 1
+        p.dt_request = 0.25
+        return p
     p = sph.preset("bubble2m")
     if name == "bubble524k":
         p.nx = p.ny = 66
@@ -285,7 +298,7 @@ def run_ours(args):
     nbytes = len(fields) * 4 * N
 
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not args.no_cpu and args.workload == "bubble2m":
         ps = cpu_sample_params()
         st = oracle_initial_state(ps)
         nsteps = args.cpu_steps
@@ -300,7 +313,7 @@ def run_ours(args):
     ctl = sim.control()
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "metric": metric_for(p), "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload_string(args.workload),
@@ -451,7 +464,8 @@ def parse_args(argv=None):
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=0, help="0: about 12 s of oracle steps")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="bubble2m", choices=["bubble2m", "bubble524k", "ensemble64", "adjoint262k"])
+    ap.add_argument("--workload", default="bubble2m",
+                    choices=["bubble2m", "bubble524k", "reference128", "ensemble64", "adjoint262k"])
     ap.add_argument("--no-tune", action="store_true", help="ensemble64: skip the autotuner")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
