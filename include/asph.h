@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define ASPH_ABI_VERSION 1
+#define ASPH_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 #define ASPH_OK             0
@@ -139,6 +139,8 @@ typedef struct AsphControl {
     int32_t surf_count;     /* particles in the lowest layer at the last sort */
     int32_t deferred;       /* targets the last brick density pass left to its
                                warp-per-target kernel (outside the staged bricks) */
+    int32_t split_regions;  /* brick regions the last density pass split into halves
+                               because they overflowed the staging capacity */
 } AsphControl;
 
 /* ---- library / parameters ---------------------------------------------- */
@@ -238,7 +240,7 @@ int asph_get_option(asph_ctx* ctx, int option, int* value);
  * by the reference's window rule, asph_h100.cu:296-327): count[i] per
  * particle (-1 if it overflowed ASPH_NBR_CAP) and list[q*N + i], q < count[i]
  * (slot-major, N*ASPH_NBR_CAP entries).  Either pointer may be NULL. */
-#define ASPH_NBR_CAP 64
+#define ASPH_NBR_CAP 192
 int asph_get_neighbours(asph_ctx* ctx, int32_t* count, int32_t* list);
 
 /* ---- diagnostics and output ----------------------------------------------- */

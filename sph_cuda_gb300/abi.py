@@ -33,7 +33,7 @@ OPT_PAIR_PATH = 1
 OPT_PAIR_SHAPE = 2
 OPT_SORT_EVERY = 3
 NOALLOC_MAX_KEYS = 524288
-NBR_CAP = 64
+NBR_CAP = 192
 PHASES = ("table_clear", "sort", "gather_kick_drift", "density_eos", "momentum_integrate", "step")
 
 _f = C.c_float
@@ -94,6 +94,7 @@ class AsphControl(C.Structure):
         ("umax", _f), ("vmax", _f), ("wmax", _f),
         ("step", _i), ("trips", _i), ("sort_count", _i), ("aborted", _i), ("clamp_pending", _i),
         ("do_sort", _i), ("error", _i), ("surf_count", _i), ("deferred", _i),
+        ("split_regions", _i),
     ]
 
 

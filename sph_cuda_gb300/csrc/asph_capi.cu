@@ -718,6 +718,7 @@ extern "C" int asph_get_control(asph_ctx* c, AsphControl* o) {
     o->step = h.step; o->trips = h.trips; o->sort_count = h.sort_count; o->aborted = h.aborted;
     o->clamp_pending = h.clamp_pending; o->do_sort = h.do_sort; o->error = h.error; o->surf_count = h.surf_count;
     o->deferred = (int32_t)h.defer_last;
+    o->split_regions = (int32_t)h.split_last;
     return ASPH_OK;
 }
 

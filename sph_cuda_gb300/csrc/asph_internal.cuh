@@ -28,6 +28,8 @@ struct DevCtl {
     unsigned defer_n;          // targets queued for the density pass's deferred kernel
     unsigned defer_done;       // finished blocks of the deferred kernel (the last resets defer_n)
     unsigned defer_last;       // targets the last density pass deferred
+    unsigned split_n;          // brick regions split into halves in the running density pass
+    unsigned split_last;       // ... in the last density pass
     unsigned gmax[3];          // float bits of |u|,|v|,|w| maxima (atomicMax)
     unsigned done;             // finished-block counter of the momentum pass
     unsigned epoch;            // radix look-back epoch

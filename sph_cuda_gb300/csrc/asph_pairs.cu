@@ -52,8 +52,24 @@ struct BrickGeom {
     static constexpr int RX = BX + 2 * H, RY = BY + 2 * H, RZ = BZ + 2 * H;
     static constexpr int R = RX * RY * RZ;
     static constexpr int KEYS = BX * BY * BZ;
-    static constexpr int LOG2K = KEYS == 512 ? 9 : KEYS == 256 ? 8 : KEYS == 128 ? 7 : 6;
+    static constexpr int LOG2K = KEYS >= 512 ? 9 : KEYS >= 256 ? 8 : KEYS >= 128 ? 7 : KEYS >= 64 ? 6
+                               : KEYS >= 32 ? 5 : KEYS >= 16 ? 4 : 3;
     static_assert((1 << LOG2K) == KEYS, "brick key count is a power of two");
+};
+
+// The two Morton-aligned halves of a brick: the top bit of a brick-local
+// key is z's for a cube, y's for BX = BY = 2 BZ and x's for BX = 2 BY = 2 BZ,
+// so the lower half of the brick's keys is the half with the smaller
+// coordinate along that axis, and each half is again a contiguous span of
+// the sorted order.
+template <int BX, int BY, int BZ>
+struct BrickHalves {
+    static constexpr bool cube = BX == BY && BY == BZ;
+    static constexpr bool flat = BX == BY && BX == 2 * BZ;   // next split along y
+    static constexpr int X = cube || flat ? BX : BX / 2;
+    static constexpr int Y = flat ? BY / 2 : BY;
+    static constexpr int Z = cube ? BZ / 2 : BZ;
+    static constexpr int DX = BX - X, DY = BY - Y, DZ = BZ - Z;   // offset of the upper half
 };
 
 struct PairCfg {
@@ -137,15 +153,15 @@ __device__ __forceinline__ void row_span(const int* s_off, int la_m2, int& k, in
 
 // Region-local window of a target: returns false if it leaves the region.
 template <int BX, int BY, int BZ, int H>
-__device__ __forceinline__ bool local_window(const Phys& P, int bxi, int byi, int bzi, float x, float y, float z,
+__device__ __forceinline__ bool local_window(const Phys& P, int ox, int oy, int oz, float x, float y, float z,
                                              int& lx, int& ly, int& zlo, int& zhi) {
     using G = BrickGeom<BX, BY, BZ, H>;
     const int ix = cell_ix(x, P.inv_dx, P.nx), iy = cell_ix(y, P.inv_dy, P.ny), iz = cell_ix(z, P.inv_dz, P.nz);
-    lx = ix - (bxi * BX - H);
+    lx = ix - (ox - H);
     lx += lx < 0 ? P.nx : 0; lx -= lx >= P.nx ? P.nx : 0;
-    ly = iy - (byi * BY - H);
+    ly = iy - (oy - H);
     ly += ly < 0 ? P.ny : 0; ly -= ly >= P.ny ? P.ny : 0;
-    const int rz0 = bzi * BZ - H;
+    const int rz0 = oz - H;
     zlo = max(iz - STENCIL, 0) - rz0;
     zhi = min(iz + STENCIL, P.nz - 1) - rz0;
     return lx >= STENCIL && lx < G::RX - STENCIL && ly >= STENCIL && ly < G::RY - STENCIL && zlo >= 0 &&
@@ -160,11 +176,11 @@ __device__ __forceinline__ bool local_window(const Phys& P, int bxi, int byi, in
 // over the block with four in flight per thread; the scan runs in shared
 // memory.
 template <int BX, int BY, int BZ, int H>
-__device__ int region_offsets(const Phys& P, const int2* __restrict__ range, int bxi, int byi, int bzi, int* s_off,
+__device__ int region_offsets(const Phys& P, const int2* __restrict__ range, int ox, int oy, int oz, int* s_off,
                               int* s_start, unsigned short* s_cell, int cap, int* s_warp) {
     using G = BrickGeom<BX, BY, BZ, H>;
     const int T = blockDim.x;
-    const int rx0 = bxi * BX - H, ry0 = byi * BY - H, rz0 = bzi * BZ - H;
+    const int rx0 = ox - H, ry0 = oy - H, rz0 = oz - H;
     for (int lb = threadIdx.x; lb < G::R; lb += 4 * T) {
         int2 rg[4];
 #pragma unroll
@@ -281,38 +297,64 @@ __global__ __launch_bounds__(256) void k_density_global(const __grid_constant__ 
     density_eos_epilogue(P, A.out, i, pi, s, rr, dt);
 }
 
-template <int BX, int BY, int BZ, int H>
-__global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ Phys P, const __grid_constant__ DArgs A,
-                                                       PairCfg C) {
+// Pointers into the density pass's dynamic shared memory.
+struct DSmem {
+    float4* sp;               // staged particles: x, y, z in cell units, rho_old
+    int* s_gidx;              // global index of a staged slot
+    int* s_off;               // region cell -> first slot (R + 1)
+    int* s_start;             // region cell -> first global index (R)
+    unsigned short* s_cell;   // slot -> region cell (cap)
+    unsigned short* s_list;   // drain queue, DLIST x T (reuses s_start and s_cell after staging)
+    int* s_warp;
+    int* s_work;              // work items {ox, oy, oz, ts, te}: the root, then two per split level
+};
+constexpr int DENSITY_SPLITS = 2;   // an overflowing brick is split into halves, then quarters
+
+// The work item at M.s_work + 5 * slot: the targets [ts, te) of the
+// Morton-aligned brick with origin (ox, oy, oz) cells.  Stage the region,
+// walk and drain.  A region that overflows the staging capacity is split
+// into its two halves (each its own region and a contiguous sub-span of the
+// targets), SPLITS times at most; targets the staged region still does not
+// cover go to the deferred pass.  Work items live in shared memory, so
+// nothing stays in registers across the first half's pass.
+template <int BX, int BY, int BZ, int H, int SPLITS>
+__device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, const PairCfg& C, const DSmem& M,
+                                               int slot) {
     using G = BrickGeom<BX, BY, BZ, H>;
-    extern __shared__ __align__(16) unsigned char smem[];
     const int T = blockDim.x;
-    float4* sp = reinterpret_cast<float4*>(smem);                       // x, y, z in cell units, rho_old
-    int* s_gidx = reinterpret_cast<int*>(sp + C.cap);                    // global index of a staged slot
-    int* s_off = s_gidx + C.cap;                                         // R + 1
-    int* s_start = s_off + (G::R + 1);                                   // R
-    unsigned short* s_cell = reinterpret_cast<unsigned short*>(s_start + G::R);   // cap: region cell of a slot
-    // the drain queue reuses s_start and s_cell, which are only needed while staging
-    unsigned short* s_list = reinterpret_cast<unsigned short*>(s_start);      // DLIST x T
-    __shared__ int s_warp[32];
-    __shared__ int s_span[2];
-    __shared__ int s_run;
-    if (threadIdx.x == 0) s_run = A.ctl->aborted ? 0 : 1;   // one decision per block (barriers follow)
+    // the work item was written by thread 0 before the call, and the shared
+    // arrays of an earlier region are no longer read
     __syncthreads();
-    if (!s_run) return;
-    const int b = blockIdx.x;
-    const int bxi = b % C.nbx, byi = (b / C.nbx) % C.nby, bzi = b / (C.nbx * C.nby);
-    if (threadIdx.x == 0) {
-        const int2 sp2 =
-            A.spans[morton3((uint32_t)(bxi * BX), (uint32_t)(byi * BY), (uint32_t)(bzi * BZ)) >> G::LOG2K];
-        s_span[0] = sp2.x;
-        s_span[1] = sp2.y;
-    }
+    const int* w = M.s_work + 5 * slot;
+    const int ox = w[0], oy = w[1], oz = w[2], ts = w[3], te = w[4];
     const float dt = A.ctl->dt;
+    float4* sp = M.sp;
+    int* s_gidx = M.s_gidx;
+    int* s_off = M.s_off;
+    int* s_start = M.s_start;
+    unsigned short* s_cell = M.s_cell;
+    unsigned short* s_list = M.s_list;
 
     // ---- stage the region: counts, scan (row-major by region cell), copy
-    const int total = region_offsets<BX, BY, BZ, H>(P, A.range, bxi, byi, bzi, s_off, s_start, s_cell, C.cap, s_warp);
+    const int total = region_offsets<BX, BY, BZ, H>(P, A.range, ox, oy, oz, s_off, s_start, s_cell, C.cap, M.s_warp);
     const bool staged = total <= C.cap;
+    if constexpr (SPLITS > 0) {
+        if (!staged) {
+            using S = BrickHalves<BX, BY, BZ>;
+            const int c0 = 1 + 2 * (DENSITY_SPLITS - SPLITS);   // this level's two child slots
+            if (threadIdx.x == 0) {
+                atomicAdd(&A.ctl->split_n, 1u);
+                const uint32_t half = morton3((uint32_t)ox, (uint32_t)oy, (uint32_t)oz) + (uint32_t)(G::KEYS / 2);
+                const int mid = ts + lower_bound_u32(A.skeys + ts, te - ts, half);
+                int* a = M.s_work + 5 * c0;
+                a[0] = ox; a[1] = oy; a[2] = oz; a[3] = ts; a[4] = mid;
+                a[5] = ox + S::DX; a[6] = oy + S::DY; a[7] = oz + S::DZ; a[8] = mid; a[9] = te;
+            }
+            density_region<S::X, S::Y, S::Z, H, SPLITS - 1>(P, A, C, M, c0);       // (starts with a barrier)
+            density_region<S::X, S::Y, S::Z, H, SPLITS - 1>(P, A, C, M, c0 + 1);
+            return;
+        }
+    }
     if (staged) {
         // slots strided over the block, four loads in flight per thread
         for (int kb = threadIdx.x; kb < total; kb += 4 * T) {
@@ -341,7 +383,6 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
     __syncthreads();
 
     // ---- targets, one warp-synchronous round of 32 targets at a time
-    const int ts = s_span[0], te = s_span[1];
     const int lane = threadIdx.x & 31;
     for (int base = ts + (threadIdx.x & ~31); base < te; base += T) {
         const int i = base + lane;
@@ -356,7 +397,7 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
             pi = A.pos[i];
             ci = to_cells(P, pi.x, pi.y, pi.z);
             rr = snd_eval(P.snd_rho, P.snd_n, pi.z);
-            fast = staged && local_window<BX, BY, BZ, H>(P, bxi, byi, bzi, pi.x, pi.y, pi.z, lx, ly, zlo, zhi);
+            fast = staged && local_window<BX, BY, BZ, H>(P, ox, oy, oz, pi.x, pi.y, pi.z, lx, ly, zlo, zhi);
         }
         // targets the staged region does not cover go to the deferred pass
         const unsigned dm = __ballot_sync(0xffffffffu, active && !fast);
@@ -430,6 +471,40 @@ __global__ __launch_bounds__(512) void k_density_brick(const __grid_constant__ P
             density_eos_epilogue(P, A.out, i, pi, s, rr, dt);
         }
     }
+}
+
+// 48 registers keep 4 blocks of up to 320 threads per SM (the shared-memory
+// limit at the default staging capacity).
+template <int BX, int BY, int BZ, int H>
+__global__ __maxnreg__(48) void k_density_brick(const __grid_constant__ Phys P, const __grid_constant__ DArgs A,
+                                                       PairCfg C) {
+    using G = BrickGeom<BX, BY, BZ, H>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int T = blockDim.x;
+    __shared__ int s_warp[32];
+    __shared__ int s_work[5 * (1 + 2 * DENSITY_SPLITS)];
+    __shared__ int s_run;
+    DSmem M;
+    M.sp = reinterpret_cast<float4*>(smem);
+    M.s_gidx = reinterpret_cast<int*>(M.sp + C.cap);
+    M.s_off = M.s_gidx + C.cap;
+    M.s_start = M.s_off + (G::R + 1);
+    M.s_cell = reinterpret_cast<unsigned short*>(M.s_start + G::R);
+    M.s_list = reinterpret_cast<unsigned short*>(M.s_start);
+    M.s_warp = s_warp;
+    M.s_work = s_work;
+    (void)T;
+    if (threadIdx.x == 0) s_run = A.ctl->aborted ? 0 : 1;   // one decision per block (barriers follow)
+    __syncthreads();
+    if (!s_run) return;
+    const int b = blockIdx.x;
+    const int bxi = b % C.nbx, byi = (b / C.nbx) % C.nby, bzi = b / (C.nbx * C.nby);
+    if (threadIdx.x == 0) {
+        const int2 sp2 =
+            A.spans[morton3((uint32_t)(bxi * BX), (uint32_t)(byi * BY), (uint32_t)(bzi * BZ)) >> G::LOG2K];
+        s_work[0] = bxi * BX; s_work[1] = byi * BY; s_work[2] = bzi * BZ; s_work[3] = sp2.x; s_work[4] = sp2.y;
+    }
+    density_region<BX, BY, BZ, H, DENSITY_SPLITS>(P, A, C, M, 0);   // (starts with a barrier)
 }
 
 // Deferred pass: one warp per queued target.  The lanes read the ranges of
@@ -559,6 +634,8 @@ __global__ __launch_bounds__(DEF_TPB) void k_density_deferred(const __grid_const
             if (atomicAdd(&ctl->defer_done, 1u) == gridDim.x - 1) {
                 ctl->defer_last = ctl->defer_n;
                 ctl->defer_n = 0u;
+                ctl->split_last = ctl->split_n;
+                ctl->split_n = 0u;
                 ctl->defer_done = 0u;
             }
         }
@@ -741,6 +818,23 @@ struct Launch {
     size_t smem;
 };
 
+// Shared memory per SM and reserved per block (queried once; GB300 values as fallback).
+void smem_limits(int* per_sm, int* reserved) {
+    static int sm = 0, res = -1;
+    if (!sm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess || sm <= 0)
+            sm = 228 * 1024;
+        if (cudaDeviceGetAttribute(&res, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess || res < 0)
+            res = 1024;
+    }
+    *per_sm = sm;
+    *reserved = res;
+}
+
+constexpr int DENSITY_REGS = 48;   // the brick kernel's register cap (__maxnreg__)
+
 Launch plan(const Phys& P, const Shape& s, int h) {
     Launch L;
     L.C.nbx = (P.nx + s.bx - 1) / s.bx;
@@ -749,17 +843,37 @@ Launch plan(const Phys& P, const Shape& s, int h) {
     L.C.nbricks = L.C.nbx * L.C.nby * L.C.nbz;
     const double ppc = (double)P.N / (double)P.ncell;
     const int R = region_cells(s, h);
-    int cap = (int)(R * ppc * STAGE_MARGIN) + 64;
-    cap = (cap + 63) & ~63;
-    L.C.cap = cap > MAX_STAGE ? MAX_STAGE : cap;
     // about one thread per expected target (the lattice keeps brick counts
     // close to the mean), in whole warps, 64..512
     int t = (int)(s.bx * s.by * s.bz * ppc * 1.04 + 31) / 32 * 32;
     L.threads = t < 64 ? 64 : (t > 512 ? 512 : t);
     // s_start (R ints) and s_cell (cap shorts) while staging; the drain queue after
-    const size_t queue = (size_t)DLIST * L.threads * 2, start = (size_t)4 * R + (size_t)2 * L.C.cap;
-    L.smem = (size_t)L.C.cap * 16 + (size_t)L.C.cap * 4 + (size_t)4 * (R + 1) +
-             ((queue > start ? queue : start) + 15) / 16 * 16;
+    const size_t queue = (size_t)DLIST * L.threads * 2;
+    auto smem_for = [&](size_t cap) {
+        const size_t start = (size_t)4 * R + 2 * cap;
+        return cap * 16 + cap * 4 + (size_t)4 * (R + 1) + ((queue > start ? queue : start) + 15) / 16 * 16;
+    };
+    // staging capacity: at least the expected region count times STAGE_MARGIN;
+    // beyond that, all the shared memory that the most resident blocks (as the
+    // registers allow) leave, so that clustered bricks overflow less often
+    // (an overflowing brick is split into halves)
+    int need = (int)(R * ppc * STAGE_MARGIN) + 64;
+    need = (need + 63) & ~63;
+    need = need > MAX_STAGE ? MAX_STAGE : need;
+    int per_sm, reserved;
+    smem_limits(&per_sm, &reserved);
+    const int by_regs = 65536 / (DENSITY_REGS * L.threads);
+    int cap = need;
+    for (int b = by_regs < 8 ? by_regs : 8; b >= 1; --b) {
+        const size_t budget = (size_t)(per_sm / b - reserved - 512);   // 512: the kernel's static arrays
+        if (smem_for(need) > budget) continue;
+        int c = MAX_STAGE;
+        while (c > need && smem_for(c) > budget) c -= 64;
+        cap = c;
+        break;
+    }
+    L.C.cap = cap;
+    L.smem = smem_for(cap);
     return L;
 }
 
@@ -779,6 +893,7 @@ template <int BX, int BY, int BZ, int H>
 void launch_dh(const Phys& P, const DArgs& A, cudaStream_t s) {
     const Launch L = plan(P, Shape{BX, BY, BZ}, H);
     cudaFuncSetAttribute(k_density_brick<BX, BY, BZ, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+    cudaFuncSetAttribute(k_density_brick<BX, BY, BZ, H>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     k_density_brick<BX, BY, BZ, H><<<L.C.nbricks, L.threads, L.smem, s>>>(P, A, L.C);
     k_density_deferred<<<deferred_blocks(), DEF_TPB, 0, s>>>(P, A);
 }

@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_layout_and_version():
     lib = abi.load_library()
-    assert lib.asph_abi_version() == 1
+    assert lib.asph_abi_version() == 2
     assert lib.asph_params_size() == ctypes.sizeof(abi.AsphParams)
     assert lib.asph_status_string(3) == b"CFL trip limit exceeded"
 

@@ -45,6 +45,9 @@ def _case(name):
     if name == "cfg_wide":   # the largest brick shape on a wider grid
         p = small_config(lat=(24, 24, 24), grid=(30, 30, 60), box=(6000.0, 6000.0, 3000.0))
         return p, random_state(p, 12, "jitter")
+    if name == "cfg_wide_cluster":   # dense blobs: staged regions overflow, split into halves and quarters
+        p = small_config(lat=(24, 24, 24), grid=(30, 30, 60), box=(6000.0, 6000.0, 3000.0))
+        return p, random_state(p, 14, "cluster")
     raise ValueError(name)
 
 
@@ -171,7 +174,8 @@ def _stages(p, s, simt=1500.0, global_path=False, tol=None):
     sim.close()
 
 
-@pytest.mark.parametrize("name", ["ref_jitter", "ref_cluster", "ref_fast", "cfg_jitter", "cfg_uniform", "cfg_wide"])
+@pytest.mark.parametrize("name", ["ref_jitter", "ref_cluster", "ref_fast", "cfg_jitter", "cfg_uniform", "cfg_wide",
+                                  "cfg_wide_cluster"])
 @pytest.mark.parametrize("path", ["brick", "global", "warp"])
 def test_stages_match_oracle(name, path):
     # ref_fast moves particles by more than a cell (250-500 m/s, far outside
@@ -397,10 +401,10 @@ def _lists_after_density(p, s, global_path):
     st = sim.get_state(("x", "y", "z"))
     cr = sim.get_sort()["cell_range"]
     sim.density_eos()
-    deferred = sim.control()["deferred"]
+    deferred = sim.control()["deferred"], sim.control()["split_regions"]
     cnt, lst = sim.neighbours()
     sim.close()
-    sets = [np.sort(lst[:c, i]) for i, c in enumerate(cnt)]
+    sets = [np.sort(lst[:c, i]) if c >= 0 else None for i, c in enumerate(cnt)]   # -1: more than the cap
     return st, cr, cnt, sets, lst, deferred
 
 
@@ -426,7 +430,7 @@ def _window_rule(p, st, cr, i):
     return out
 
 
-@pytest.mark.parametrize("name", ["cfg_jitter", "ref_fast", "cfg_wide"])
+@pytest.mark.parametrize("name", ["cfg_jitter", "ref_fast", "cfg_wide", "cfg_wide_cluster"])
 def test_neighbour_lists_exact(name):
     p, s = _case(name)
     st_b, cr, cnt_b, sets_b, lst_b, deferred = _lists_after_density(p, s, 0)
@@ -435,18 +439,24 @@ def test_neighbour_lists_exact(name):
     assert np.array_equal(st_b["x"], st_g["x"]) and np.array_equal(st_w["x"], st_g["x"])
     assert np.array_equal(cnt_b, cnt_g) and np.array_equal(cnt_w, cnt_g)
     for i in range(p.n_particles):
-        assert np.array_equal(sets_b[i], sets_g[i]), i
+        if cnt_g[i] >= 0:
+            assert np.array_equal(sets_b[i], sets_g[i]), i
     # all three paths list each target's neighbours in the reference's loop order
     n = np.where(cnt_g < 0, 0, cnt_g)
     slot = np.arange(lst_g.shape[0])[:, None] < n[None, :]
     assert np.array_equal(np.where(slot, lst_b, -1), np.where(slot, lst_g, -1))
     assert np.array_equal(np.where(slot, lst_w, -1), np.where(slot, lst_g, -1))
     if name == "ref_fast":   # moved by more than a cell: the brick pass deferred some targets
-        assert deferred > 0
+        assert deferred[0] > 0
+    if name == "cfg_wide_cluster":   # overflowing regions were split before anything was deferred
+        assert deferred[1] > 0
     # the window rule in float32 on a sample of targets
     rng = np.random.default_rng(0)
     for i in rng.choice(p.n_particles, size=min(300, p.n_particles), replace=False):
         ref = _window_rule(p, st_b, cr, i)
+        if cnt_b[i] < 0:   # no list: more neighbours than the cap (momentum walks the table instead)
+            assert len(ref) >= abi.NBR_CAP, (i, len(ref))
+            continue
         got = set(sets_b[i].tolist())
         for j, r2 in ref.items():
             assert j in got or abs(r2 - 4.0) < 1e-4, (i, j, r2)
