@@ -156,7 +156,9 @@ def workload_string(name: str) -> str:
     return {"bubble2m": "moist bubble, 2,097,152 particles, 133x133x200 cells, sort every step",
             "bubble524k": "moist bubble, 524,288 particles, 66x66x200 cells, sort every step",
             "reference128": "the reference's own geometry and init, 128x128x128 cells, dt 0.25 s, "
-                            "sort every step"}[name]
+                            "sort every step",
+            "large16m": "large anisotropic run, 16,777,216 particles, 250x250x500 cells (h 160 m x 20 m), "
+                        "95% RH boundary layer, theta noise 0.2 K, sort every step"}[name]
 
 
 def metric_for(p) -> str:
@@ -197,8 +199,11 @@ def workload_params(name: str):
     bubble524k: the same physics, cell size and density on a 10 x 10 x 8 km box
     (64 x 64 x 128 lattice, 66 x 66 x 200 cells) for profiler captures.
     reference128: the reference's own configuration at --nx --ny --nz 128 and
-    --dt 0.25 with a sort every step (what oracle/time_reference.py native runs)."""
+    --dt 0.25 with a sort every step (what oracle/time_reference.py native runs).
+    large16m: the 16,777,216-particle anisotropic run (40 x 40 x 10 km, 8:1)."""
     import sph_cuda_gb300 as sph
+    if name == "large16m":
+        return sph.preset("large16m")
     if name == "reference128":
         p = sph.preset("reference", 128, 128, 128)
         p.sort_every = 1
@@ -230,6 +235,8 @@ def run_ours(args):
     N, C = p.n_particles, p.nx * p.ny * p.nz
     sim = sph.Asph(p, stream=stream.cuda_stream)
     sim.init()
+    if args.advance > 0:   # untimed steps first: measure the developed state
+        sim.step(args.advance)
     sim.step(max(args.warmup, 1))
     per_step = sim.step_kernels()   # kernel nodes of the step's CUDA graph
 
@@ -317,7 +324,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload_string(args.workload),
-                       "particles": N, "cells": C, "dt_s": ctl["dt"],
+                       "particles": N, "cells": C, "dt_s": ctl["dt"], "advance_steps": args.advance,
                        "l2": "working set %.0f MB > 129 MB L2 (no flush needed)" % ((N * 164 + C * 20) / 1e6),
                        "parallelism": "replicas x%d" % ws},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -459,13 +466,15 @@ def run_adjoint(args):
 def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=500)   # the moist bubble's 500 steps
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=0, help="0: about 12 s of oracle steps")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--advance", type=int, default=0,
+                    help="untimed steps after init, before warm-up (profile a developed state)")
     ap.add_argument("--workload", default="bubble2m",
-                    choices=["bubble2m", "bubble524k", "reference128", "ensemble64", "adjoint262k"])
+                    choices=["bubble2m", "bubble524k", "reference128", "large16m", "ensemble64", "adjoint262k"])
     ap.add_argument("--no-tune", action="store_true", help="ensemble64: skip the autotuner")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
