@@ -31,6 +31,8 @@
 // and reverses it.
 #include <stdio.h>
 #include <string.h>
+#include <map>
+#include <utility>
 #include <vector>
 #include "asph_ctx.cuh"
 #include "asph_device.cuh"
@@ -608,6 +610,13 @@ __global__ void k_adj_integrate(const Phys P, float dt, float Ts, float qs_sfc, 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// A captured window step: its graph and the ping-pong indices it leaves.
+struct AfGraph {
+    cudaGraphExec_t exec = nullptr;
+    int pc = 0, vc = 0, qc = 0, rc = 0;
+    bool lists_valid = false;
+};
+
 struct asph_adj {
     asph_ctx* c = nullptr;
     int K = 0, every = 0, nseg = 0;
@@ -622,7 +631,17 @@ struct asph_adj {
     AdjBufs A;
     std::vector<void*> mem;
     bool forward_done = false;
+    // window steps as CUDA graphs, keyed by (tape slot or -1, ping-pong state); valid for the
+    // window physics and the context's option epoch they were captured with
+    std::map<std::pair<int, int>, AfGraph> graphs;
+    Phys graphs_P;
+    unsigned graphs_epoch = 0;
+    void drop_graphs() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
+        graphs.clear();
+    }
     ~asph_adj() {
+        drop_graphs();
         for (auto* s : ckpt) asph_snapshot_destroy(s);
         if (last) asph_snapshot_destroy(last);
         for (void* p : mem) cudaFree(p);
@@ -700,6 +719,42 @@ int check_window(asph_adj* a) {
     if (st) return st;
     if (ctl.trips > a->trips0 || ctl.clamp_pending)
         return fail(ASPH_ERR_STATE, "a CFL trip inside the adjoint window (velocity clamp is not differentiated)");
+    return ASPH_OK;
+}
+
+// One window step through its captured graph (captured on first use).
+int af_step_graph(asph_adj* a, int slot) {
+    asph_ctx* c = a->c;
+    if (memcmp(&a->graphs_P, &a->P, sizeof(Phys)) != 0 || a->graphs_epoch != c->graph_epoch) {
+        a->drop_graphs();
+        a->graphs_P = a->P;
+        a->graphs_epoch = c->graph_epoch;
+    }
+    const std::pair<int, int> key(slot, graph_slot(c->B));
+    auto it = a->graphs.find(key);
+    if (it == a->graphs.end()) {
+        const Bufs before = c->B;
+        cudaGraph_t g = nullptr;
+        CKR(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        const int st = af_step(a, slot >= 0 ? &a->tape[slot] : nullptr);
+        const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        AfGraph ag;
+        ag.pc = c->B.pc; ag.vc = c->B.vc; ag.qc = c->B.qc; ag.rc = c->B.rc;
+        ag.lists_valid = c->lists_valid;
+        c->B = before;
+        if (st) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return fail(ASPH_ERR_CUDA, "adjoint graph capture: %s", cudaGetErrorString(e));
+        const cudaError_t ei = cudaGraphInstantiate(&ag.exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) return fail(ASPH_ERR_CUDA, "adjoint graph instantiate: %s", cudaGetErrorString(ei));
+        it = a->graphs.emplace(key, ag).first;
+    }
+    CKR(cudaGraphLaunch(it->second.exec, c->stream));
+    c->B.pc = it->second.pc; c->B.vc = it->second.vc; c->B.qc = it->second.qc; c->B.rc = it->second.rc;
+    c->lists_valid = it->second.lists_valid;
     return ASPH_OK;
 }
 
@@ -794,7 +849,7 @@ extern "C" int asph_adj_forward(asph_adj* a) {
         if ((st = asph_snapshot_save(c, a->ckpt[sgm]))) return st;
         const int n = (sgm == a->nseg - 1) ? a->K - sgm * a->every : a->every;
         for (int k = 0; k < n; ++k)
-            if ((st = af_step(a, nullptr))) return st;
+            if ((st = af_step_graph(a, -1))) return st;
     }
     if ((st = asph_snapshot_save(c, a->last))) return st;
     if ((st = check_window(a))) return st;
@@ -838,7 +893,7 @@ extern "C" int asph_adj_backward(asph_adj* a, const float* dL_dqc, const float* 
         if ((st = asph_snapshot_restore(c, a->ckpt[sgm]))) break;
         for (int k = 0; k < n && !st; ++k) {
             a->tape[k].simt = a->simt0 + (double)a->dt * (double)(sgm * a->every + k);
-            st = af_step(a, &a->tape[k]);
+            st = af_step_graph(a, k);
         }
         for (int k = n - 1; k >= 0 && !st; --k) reverse_step(a, a->tape[k], s);
         CKR(cudaGetLastError());

@@ -419,6 +419,7 @@ extern "C" int asph_set_option(asph_ctx* c, int option, int value) {
     }
     for (auto& g : c->gexec)   // captured graphs hold the old kernels and parameters
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    ++c->graph_epoch;
     if (option != ASPH_OPT_SORT_EVERY) c->spans_valid = false;   // spans are per brick shape
     return ASPH_OK;
 }

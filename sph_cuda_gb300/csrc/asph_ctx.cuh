@@ -20,6 +20,7 @@ struct asph_ctx {
     // graphs keyed by the ping-pong state at the start of the step
     cudaGraphExec_t gexec[16] = {};
     int graph_kernels = 0;      // kernel nodes of a captured step graph
+    unsigned graph_epoch = 0;   // bumped whenever an option change drops the captured graphs
     // staging for host <-> device SoA copies (16 floats per particle)
     float* stage = nullptr;
     // audit
