@@ -336,6 +336,7 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     AL(B.defer, N * 4);
     sort_inc_sizes(P.N, &B.inc_max, &B.inc_tiles, &B.inc_blocks);
     AL(B.inc_u, N * 4);
+    AL(B.inc_uk, N * 4);
     for (int k = 0; k < 2; ++k) {
         AL(B.inc_k[k], (size_t)B.inc_max * 4);
         AL(B.inc_i[k], (size_t)B.inc_max * 4);

@@ -61,6 +61,7 @@ struct Bufs {
     // incremental sort: unchanged indices, changed keys/indices (ping-pong),
     // per-block counts, the changed-key sort's look-back words
     uint32_t* inc_u;
+    uint32_t* inc_uk;   // the unchanged particles' keys, in the order of inc_u
     uint32_t* inc_k[2];
     uint32_t* inc_i[2];
     uint32_t* inc_cnt;

@@ -340,8 +340,8 @@ __global__ void k_inc_scan(uint32_t* __restrict__ cnt, int nblocks, int inc_max,
 __global__ __launch_bounds__(INC_TPB) void k_inc_split(const uint32_t* __restrict__ kin,
                                                        const uint32_t* __restrict__ sprev, int N,
                                                        const uint32_t* __restrict__ off, uint32_t* __restrict__ uidx,
-                                                       uint32_t* __restrict__ ck, uint32_t* __restrict__ ci,
-                                                       const DevCtl* __restrict__ ctl) {
+                                                       uint32_t* __restrict__ ukey, uint32_t* __restrict__ ck,
+                                                       uint32_t* __restrict__ ci, const DevCtl* __restrict__ ctl) {
     if (!inc_step_sorts(ctl) || !ctl->inc_on) return;
     __shared__ uint32_t s_warp[INC_TPB / 32];
     const int base = blockIdx.x * INC_CHUNK;
@@ -370,6 +370,7 @@ __global__ __launch_bounds__(INC_TPB) void k_inc_split(const uint32_t* __restric
             ci[oc + rc] = (uint32_t)e;
         } else if (in) {
             uidx[ou + ru] = (uint32_t)e;
+            ukey[ou + ru] = k;
         }
         oc += total;
         ou += (uint32_t)min(INC_TPB, max(0, N - (base + r))) - total;
@@ -377,47 +378,59 @@ __global__ __launch_bounds__(INC_TPB) void k_inc_split(const uint32_t* __restric
     }
 }
 
-// Merge of the unchanged sequence (uidx, keys kin[uidx]) and the sorted
-// changed sequence (ck, ci) by (key, index): merge path, MERGE_ITEMS outputs
-// per thread.
+// Merge of the unchanged sequence (uidx, keys ukey) and the sorted changed
+// sequence (ck, ci) by (key, index): merge path, MERGE_ITEMS outputs per
+// thread, staged in shared memory so that the block writes its tile of the
+// output coalesced.  The split wrote the unchanged keys beside their indices,
+// so a merge-path probe is one load, not a dependent pair.
 __device__ __forceinline__ bool key_idx_less(uint32_t ka, uint32_t ia, uint32_t kb, uint32_t ib) {
     return ka < kb || (ka == kb && ia < ib);
 }
 __global__ __launch_bounds__(INC_TPB) void k_inc_merge(const uint32_t* __restrict__ uidx,
-                                                       const uint32_t* __restrict__ kin,
+                                                       const uint32_t* __restrict__ ukey,
                                                        const uint32_t* __restrict__ ck,
                                                        const uint32_t* __restrict__ ci, int N,
                                                        uint32_t* __restrict__ skeys, uint32_t* __restrict__ perm,
                                                        const DevCtl* __restrict__ ctl) {
     if (!inc_step_sorts(ctl) || !ctl->inc_on) return;
+    __shared__ uint32_t s_k[INC_TPB * MERGE_ITEMS], s_i[INC_TPB * MERGE_ITEMS];
     const int m = (int)ctl->inc_m, nu = N - m;
-    const long long p0 = ((long long)blockIdx.x * INC_TPB + threadIdx.x) * MERGE_ITEMS;
-    if (p0 >= N) return;
-    int lo = (int)max(0LL, p0 - nu), hi = (int)min(p0, (long long)m);
-    while (lo < hi) {   // how many changed keys come first among the first p0 outputs
-        const int mid = (lo + hi) >> 1;
-        const uint32_t ua = uidx[p0 - 1 - mid];
-        if (key_idx_less(ck[mid], ci[mid], kin[ua], ua)) lo = mid + 1;
-        else hi = mid;
+    const long long t0 = (long long)blockIdx.x * INC_TPB * MERGE_ITEMS;   // the block's first output
+    const long long p0 = t0 + (long long)threadIdx.x * MERGE_ITEMS;
+    if (p0 < N) {
+        int lo = (int)max(0LL, p0 - nu), hi = (int)min(p0, (long long)m);
+        while (lo < hi) {   // how many changed keys come first among the first p0 outputs
+            const int mid = (lo + hi) >> 1;
+            const long long u = p0 - 1 - mid;
+            if (key_idx_less(ck[mid], ci[mid], ukey[u], uidx[u])) lo = mid + 1;
+            else hi = mid;
+        }
+        int b = lo, a = (int)p0 - lo;
+        for (int j = 0; j < MERGE_ITEMS && p0 + j < N; ++j) {
+            bool take_c = b < m;
+            uint32_t ua = 0, ku = 0;
+            if (a < nu) {
+                ua = uidx[a];
+                ku = ukey[a];
+                take_c = take_c && key_idx_less(ck[b], ci[b], ku, ua);
+            }
+            const int o = threadIdx.x * MERGE_ITEMS + j;
+            if (take_c) {
+                s_k[o] = ck[b];
+                s_i[o] = ci[b];
+                ++b;
+            } else {
+                s_k[o] = ku;
+                s_i[o] = ua;
+                ++a;
+            }
+        }
     }
-    int b = lo, a = (int)p0 - lo;
-    for (int j = 0; j < MERGE_ITEMS && p0 + j < N; ++j) {
-        bool take_c = b < m;
-        uint32_t ua = 0, ku = 0;
-        if (a < nu) {
-            ua = uidx[a];
-            ku = kin[ua];
-            take_c = take_c && key_idx_less(ck[b], ci[b], ku, ua);
-        }
-        if (take_c) {
-            skeys[p0 + j] = ck[b];
-            perm[p0 + j] = ci[b];
-            ++b;
-        } else {
-            skeys[p0 + j] = ku;
-            perm[p0 + j] = ua;
-            ++a;
-        }
+    __syncthreads();
+    const int nout = (int)min((long long)INC_TPB * MERGE_ITEMS, (long long)N - t0);
+    for (int e = threadIdx.x; e < nout; e += INC_TPB) {
+        skeys[t0 + e] = s_k[e];
+        perm[t0 + e] = s_i[e];
     }
 }
 
@@ -453,7 +466,7 @@ void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s) {
                                                    B.ntiles, p, B.ctl, force, 0);
     }
     if (inc) {
-        k_inc_split<<<B.inc_blocks, INC_TPB, 0, s>>>(B.kin, B.skeys, P.N, B.inc_cnt, B.inc_u, B.inc_k[0],
+        k_inc_split<<<B.inc_blocks, INC_TPB, 0, s>>>(B.kin, B.skeys, P.N, B.inc_cnt, B.inc_u, B.inc_uk, B.inc_k[0],
                                                      B.inc_i[0] + 0, B.ctl);
         // the changed keys: stable radix sort of (key, index), lane 1
         int ib = (B.inc_max + TPB * 8 - 1) / (TPB * 8);
@@ -470,7 +483,7 @@ void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s) {
             vi = vo;
         }
         const int mb = (P.N + INC_TPB * MERGE_ITEMS - 1) / (INC_TPB * MERGE_ITEMS);
-        k_inc_merge<<<mb, INC_TPB, 0, s>>>(B.inc_u, B.kin, ki, vi, P.N, B.skeys, B.perm, B.ctl);
+        k_inc_merge<<<mb, INC_TPB, 0, s>>>(B.inc_u, B.inc_uk, ki, vi, P.N, B.skeys, B.perm, B.ctl);
     }
 }
 
