@@ -316,6 +316,15 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     const Phys& P = c->P;
     Bufs& B = c->B;
     memset(&B, 0, sizeof(B));
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&B.aux, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B.ev_fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B.ev_join, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            delete c;
+            return fail(ASPH_ERR_CUDA, "stream create: %s", cudaGetErrorString(e));
+        }
+    }
     const size_t N = (size_t)P.N, C = (size_t)P.ncell;
     B.npasses = (P.key_bits + 7) / 8;
     B.ntiles = (int)((N + SORT_TILE - 1) / SORT_TILE);

@@ -11,7 +11,7 @@ using namespace asph;
 struct asph_ctx {
     AsphParams prm;
     Phys P;
-    Bufs B;
+    Bufs B{};
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool initialised = false;
@@ -56,6 +56,9 @@ struct asph_ctx {
         for (auto& g : gexec)
             if (g) cudaGraphExecDestroy(g);
         for (void* q : allocs) cudaFree(q);
+        if (B.ev_fork) cudaEventDestroy(B.ev_fork);
+        if (B.ev_join) cudaEventDestroy(B.ev_join);
+        if (B.aux) cudaStreamDestroy(B.aux);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 };

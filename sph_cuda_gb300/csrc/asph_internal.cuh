@@ -83,6 +83,8 @@ struct Bufs {
     int pc, vc, qc, rc; // current index of pos/vel/thq/rain ping-pong pairs
     int force_global;   // 1: pair passes take the per-target global path, 2: density warp per target
     int shape;          // brick shape index of the density pass, -1: automatic
+    cudaStream_t aux;   // second stream: the full sort runs beside the incremental one (a graph branch)
+    cudaEvent_t ev_fork, ev_join;
     float4* src;        // source-term hook: per-particle tendencies (theta, qv, qc), NULL when off
     float4* src_tmp;    // the tendencies in the order of the current step (written by the gather)
 };

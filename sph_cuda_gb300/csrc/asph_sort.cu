@@ -456,15 +456,26 @@ void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s) {
         k_inc_count<<<B.inc_blocks, INC_TPB, 0, s>>>(B.kin, B.skeys, P.N, B.inc_cnt, B.ctl);
         k_inc_scan<<<1, 1024, 0, s>>>(B.inc_cnt, B.inc_blocks, B.inc_max, B.ctl);
     }
+    // Exactly one of the two sorts does work; the device flag decides.  With
+    // both, the full sort runs on the second stream (in a captured step, a
+    // graph branch) so that its kernels, which then return at once, are off
+    // the incremental sort's path; they share no buffers once the flag is set.
+    const bool fork = inc && B.aux;
+    cudaStream_t fs = fork ? B.aux : s;
+    if (fork) {
+        cudaEventRecord(B.ev_fork, s);
+        cudaStreamWaitEvent(B.aux, B.ev_fork, 0);
+    }
     int hb = (P.N + TPB * 8 - 1) / (TPB * 8);
     hb = hb > 152 * 8 ? 152 * 8 : hb;
-    k_hist<<<hb, SORT_TPB, 0, s>>>(B.kin, P.N, B.npasses, B.ctl, force, 0);
+    k_hist<<<hb, SORT_TPB, 0, fs>>>(B.kin, P.N, B.npasses, B.ctl, force, 0);
     for (int p = 0; p < B.npasses; ++p) {
         const uint32_t* ki = p == 0 ? B.kin : B.kbuf[(p - 1) & 1];
         const uint32_t* vi = p == 0 ? nullptr : B.vbuf[(p - 1) & 1];
-        k_radix_pass<<<B.ntiles, SORT_TPB, 0, s>>>(ki, vi, B.kbuf[p & 1], B.vbuf[p & 1], B.status, P.N,
-                                                   B.ntiles, p, B.ctl, force, 0);
+        k_radix_pass<<<B.ntiles, SORT_TPB, 0, fs>>>(ki, vi, B.kbuf[p & 1], B.vbuf[p & 1], B.status, P.N,
+                                                    B.ntiles, p, B.ctl, force, 0);
     }
+    if (fork) cudaEventRecord(B.ev_join, B.aux);
     if (inc) {
         k_inc_split<<<B.inc_blocks, INC_TPB, 0, s>>>(B.kin, B.skeys, P.N, B.inc_cnt, B.inc_u, B.inc_uk, B.inc_k[0],
                                                      B.inc_i[0] + 0, B.ctl);
@@ -485,6 +496,7 @@ void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s) {
         const int mb = (P.N + INC_TPB * MERGE_ITEMS - 1) / (INC_TPB * MERGE_ITEMS);
         k_inc_merge<<<mb, INC_TPB, 0, s>>>(B.inc_u, B.inc_uk, ki, vi, P.N, B.skeys, B.perm, B.ctl);
     }
+    if (fork) cudaStreamWaitEvent(s, B.ev_join, 0);
 }
 
 }  // namespace asph
