@@ -43,6 +43,7 @@ namespace asph {
 constexpr int MAX_HALO = 3;      // widest staged halo (cells around a brick)
 constexpr int DLIST = 24;        // queued accepted candidates per thread (D)
 constexpr int M_TPB = 256;
+constexpr int M_TPT = 2;         // targets per thread of the momentum pass
 
 template <int BX, int BY, int BZ, int H>
 struct BrickGeom {
@@ -691,55 +692,62 @@ __global__ __launch_bounds__(M_TPB, 4) void k_momentum(const __grid_constant__ P
         const int cid = (blockIdx.x - A.part_blocks) * blockDim.x + threadIdx.x;
         if (cid < P.ncell && !aborted) rain_cell(P, cid, dt, A.rain_in, A.rain_delta, A.rain_out, A.precip);
     } else {
-        const int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i < P.N) {
-            if (aborted) {
-                if (mode & M_INTEGRATE) A.out.vel_out[i] = A.vel[i];
-            } else {
-                // (x, y, z, p') and (u, v, w, rho): packed by the density pass
-                // when the lists are current, else from the state buffers
-                float4 a, b;
-                if (A.use_lists) {
-                    a = A.ms0[i];
-                    b = A.ms1[i];
+        // M_TPT targets per thread, the lanes of warp w on targets w * 32 * M_TPT + lane + 32 r:
+        // a warp waits on the longest sum of its lanes' lists rather than on the longest list
+        // of each round
+        const int tbase = blockIdx.x * (M_TPB * M_TPT) + (threadIdx.x >> 5) * (32 * M_TPT) + (threadIdx.x & 31);
+        for (int r = 0; r < M_TPT; ++r) {
+            const int i = tbase + 32 * r;
+            if (i < P.N) {
+                if (aborted) {
+                    if (mode & M_INTEGRATE) A.out.vel_out[i] = A.vel[i];
                 } else {
-                    const float4 p = A.pos[i], v = A.vel[i];
-                    const float2 r = A.rp[i];
-                    a = make_float4(p.x, p.y, p.z, r.y);
-                    b = make_float4(v.x, v.y, v.z, r.x);
-                }
-                MTarget T;
-                T.x = a.x; T.y = a.y; T.z = a.z;
-                T.u = b.x; T.v = b.y; T.w = b.z;
-                T.rhoi = fmaxf(b.w, 1e-3f);
-                T.irhoi = __frcp_rn(T.rhoi);
-                T.pri = a.w;
-                MSum s{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                const int cnt = A.use_lists ? A.nbr_cnt[i] : -1;
-                if (cnt >= 0) {
-                    // four neighbours' loads in flight before their arithmetic
-                    int q = 0;
-                    for (; q + 4 <= cnt; q += 4) {
-                        int jj[4];
-                        float4 pp[4], vv[4];
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) jj[u] = A.nbr[(size_t)(q + u) * P.N + i];
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            pp[u] = A.ms0[jj[u]];
-                            vv[u] = A.ms1[jj[u]];
+                    // (x, y, z, p') and (u, v, w, rho): packed by the density pass
+                    // when the lists are current, else from the state buffers
+                    float4 a, b;
+                    if (A.use_lists) {
+                        a = A.ms0[i];
+                        b = A.ms1[i];
+                    } else {
+                        const float4 p = A.pos[i], v = A.vel[i];
+                        const float2 r = A.rp[i];
+                        a = make_float4(p.x, p.y, p.z, r.y);
+                        b = make_float4(v.x, v.y, v.z, r.x);
+                    }
+                    MTarget T;
+                    T.x = a.x; T.y = a.y; T.z = a.z;
+                    T.u = b.x; T.v = b.y; T.w = b.z;
+                    T.rhoi = fmaxf(b.w, 1e-3f);
+                    T.irhoi = __frcp_rn(T.rhoi);
+                    T.pri = a.w;
+                    MSum s{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                    const int cnt = A.use_lists ? A.nbr_cnt[i] : -1;
+                    if (cnt >= 0) {
+                        // four neighbours' loads in flight before their arithmetic
+                        int q = 0;
+                        for (; q + 4 <= cnt; q += 4) {
+                            int jj[4];
+                            float4 pp[4], vv[4];
+    #pragma unroll
+                            for (int u = 0; u < 4; ++u) jj[u] = A.nbr[(size_t)(q + u) * P.N + i];
+    #pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                pp[u] = A.ms0[jj[u]];
+                                vv[u] = A.ms1[jj[u]];
+                            }
+    #pragma unroll
+                            for (int u = 0; u < 4; ++u) msum_add(P, s, T, pp[u], vv[u]);
                         }
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) msum_add(P, s, T, pp[u], vv[u]);
+                        for (; q < cnt; ++q) {
+                            const int j = A.nbr[(size_t)q * P.N + i];
+                            msum_add(P, s, T, A.ms0[j], A.ms1[j]);
+                        }
+                    } else {
+                        s = momentum_target_global(P, A, T);
                     }
-                    for (; q < cnt; ++q) {
-                        const int j = A.nbr[(size_t)q * P.N + i];
-                        msum_add(P, s, T, A.ms0[j], A.ms1[j]);
-                    }
-                } else {
-                    s = momentum_target_global(P, A, T);
+                    const float3 mi = momentum_epilogue(P, A.out, i, T, s, (mode & M_INTEGRATE) != 0, dt);
+                    m = make_float3(fmaxf(m.x, mi.x), fmaxf(m.y, mi.y), fmaxf(m.z, mi.z));
                 }
-                m = momentum_epilogue(P, A.out, i, T, s, (mode & M_INTEGRATE) != 0, dt);
             }
         }
         if (mode & M_INTEGRATE) {
@@ -991,7 +999,7 @@ void launch_momentum(const Phys& P, const Bufs& B, int mode, int use_lists, cuda
     A.rain_out = B.rain[1 - B.rc];
     A.precip = B.precip;
     A.ctl = B.ctl;
-    A.part_blocks = blocks_for(P.N, M_TPB);
+    A.part_blocks = blocks_for(P.N, M_TPB * M_TPT);
     const int rain_blocks = (mode & M_RAIN) ? blocks_for(P.ncell, M_TPB) : 0;
     k_momentum<<<A.part_blocks + rain_blocks, M_TPB, 0, s>>>(P, A, mode);
 }
