@@ -22,9 +22,12 @@
 // candidates in a small per-thread list in shared memory, and drains the
 // list (density sums + neighbour-list writes) in uniform loops.  H = 2 (the
 // stencil) covers every target still in a cell of its brick; H = 3 also
-// covers one cell of drift since the sort.  A target whose window leaves
-// the staged region, or every target of a brick whose region overflows the
-// staging capacity, is queued for the deferred pass.
+// covers one cell of drift since the sort.  A region that overflows the
+// staging capacity is split into its two Morton-aligned halves (each a
+// contiguous sub-span of the targets with a smaller region), and a half
+// that overflows once more; a target whose window leaves the staged region,
+// and the targets of a quarter that still overflows, are queued for the
+// deferred pass.
 //
 // Deferred pass.  One warp per queued target: the lanes read the window's
 // cell ranges from the global table in parallel and test the candidates 32
