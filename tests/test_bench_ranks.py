@@ -77,3 +77,19 @@ def test_workload_presets_match_their_descriptions():
     assert q.dx == pytest.approx(p.dx) and q.dz == pytest.approx(p.dz)
     s = bench.cpu_sample_params()
     assert s.n_particles == 131072 and s.dx == pytest.approx(p.dx)
+
+
+def test_other_workloads_and_options():
+    r = bench.workload_params("reference128")
+    assert (r.nx, r.ny, r.nz) == (128, 128, 128) and r.n_particles == 128 ** 3
+    assert r.sort_every == 1 and r.dt_request == pytest.approx(0.25)
+    big = bench.workload_params("large16m")
+    assert big.n_particles == 256 ** 3 and (big.nx, big.ny, big.nz) == (250, 250, 500)
+    assert big.dx / big.dz == pytest.approx(8.0)
+    for name in ("bubble2m", "bubble524k", "reference128", "large16m"):
+        assert bench.workload_string(name)
+        assert bench.metric_for(bench.workload_params(name)).startswith("particle-steps/s (plain step, ")
+    assert bench.metric_for(bench.workload_params("bubble2m")) == bench.METRIC   # the headline metric string
+    a = bench.parse_args([])
+    assert a.steps == 500 and a.advance == 0 and a.workload == "bubble2m"   # the configuration's 500 steps
+    assert bench.parse_args(["--advance", "500"]).advance == 500
