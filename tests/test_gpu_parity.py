@@ -546,3 +546,18 @@ def test_brick_spans_follow_shape_changes_and_restores():
         # the pass found nearly every target in its brick
         assert a.control()["deferred"] < p.n_particles // 20, (shape, a.control()["deferred"])
     a.close()
+
+
+def test_step_kernels_count_the_step_graph():
+    """The kernel launches of a plain step, read from the captured graph: the sort preparation,
+    both sorts (the full one a graph branch; a histogram and 3 passes each at 18-bit keys, plus
+    the incremental sort's count, scan, split and merge), the gather, the density pass and its
+    deferred kernel, and momentum."""
+    p = small_config(lat=(24, 24, 24), grid=(30, 30, 60), box=(6000.0, 6000.0, 3000.0), sort_every=1)
+    sim = Asph(p)
+    sim.init()
+    n0 = sim.step_kernels()        # captured without running
+    sim.step(3)
+    passes = (3 * 6 + 7) // 8      # 6 bits per axis at 60 cells
+    assert n0 == sim.step_kernels() == 1 + (1 + passes) + (4 + 1 + passes) + 1 + 2 + 1
+    sim.close()
