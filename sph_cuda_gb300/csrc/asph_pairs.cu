@@ -175,13 +175,13 @@ __device__ __forceinline__ bool local_window(const Phys& P, int ox, int oy, int 
 // Offsets of the staged region of a brick: s_off[l] = first slot of region
 // cell l (row-major, H cells around the brick, x/y wrapped), s_off[R] =
 // the total, s_start[l] = the cell's first global index, and (when it fits,
-// total <= cap) s_cell[k] = the region cell of slot k.  A cell's particles
+// total <= cap) s_gidx[k] = the global index of slot k.  A cell's particles
 // take consecutive slots in index order.  The cell-table loads are strided
 // over the block with four in flight per thread; the scan runs in shared
 // memory.
 template <int BX, int BY, int BZ, int H>
 __device__ int region_offsets(const Phys& P, const int2* __restrict__ range, int ox, int oy, int oz, int* s_off,
-                              int* s_start, unsigned short* s_cell, int cap, int* s_warp) {
+                              int* s_start, int* s_gidx, int cap, int* s_warp) {
     using G = BrickGeom<BX, BY, BZ, H>;
     const int T = blockDim.x;
     const int rx0 = ox - H, ry0 = oy - H, rz0 = oz - H;
@@ -222,8 +222,10 @@ __device__ int region_offsets(const Phys& P, const int2* __restrict__ range, int
     for (int l = l0; l < l1; ++l) {
         const int c = s_off[l];
         s_off[l] = excl;
-        if (map)
-            for (int k = 0; k < c; ++k) s_cell[excl + k] = (unsigned short)l;
+        if (map) {
+            const int g = s_start[l];
+            for (int k = 0; k < c; ++k) s_gidx[excl + k] = g + k;
+        }
         excl += c;
     }
     if (threadIdx.x == 0) s_off[G::R] = total;
@@ -307,8 +309,7 @@ struct DSmem {
     int* s_gidx;              // global index of a staged slot
     int* s_off;               // region cell -> first slot (R + 1)
     int* s_start;             // region cell -> first global index (R)
-    unsigned short* s_cell;   // slot -> region cell (cap)
-    unsigned short* s_list;   // drain queue, DLIST x T (reuses s_start and s_cell after staging)
+    unsigned short* s_list;   // drain queue, DLIST x T (reuses s_start after staging)
     int* s_warp;
     int* s_work;              // work items {ox, oy, oz, ts, te}: the root, then two per split level
 };
@@ -336,11 +337,10 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
     int* s_gidx = M.s_gidx;
     int* s_off = M.s_off;
     int* s_start = M.s_start;
-    unsigned short* s_cell = M.s_cell;
     unsigned short* s_list = M.s_list;
 
     // ---- stage the region: counts, scan (row-major by region cell), copy
-    const int total = region_offsets<BX, BY, BZ, H>(P, A.range, ox, oy, oz, s_off, s_start, s_cell, C.cap, M.s_warp);
+    const int total = region_offsets<BX, BY, BZ, H>(P, A.range, ox, oy, oz, s_off, s_start, s_gidx, C.cap, M.s_warp);
     const bool staged = total <= C.cap;
     if constexpr (SPLITS > 0) {
         if (!staged) {
@@ -363,15 +363,10 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
         // slots strided over the block, four loads in flight per thread
         for (int kb = threadIdx.x; kb < total; kb += 4 * T) {
             float4 q[4];
-            int jg[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int k = kb + u * T;
-                if (k < total) {
-                    const int l = s_cell[k];
-                    jg[u] = s_start[l] + (k - s_off[l]);
-                    q[u] = A.pos[jg[u]];
-                }
+                if (k < total) q[u] = A.pos[s_gidx[k]];
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
@@ -379,7 +374,6 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
                 if (k < total) {
                     const float3 c = to_cells(P, q[u].x, q[u].y, q[u].z);   // compared in cell units
                     sp[k] = make_float4(c.x, c.y, c.z, q[u].w);
-                    s_gidx[k] = jg[u];
                 }
             }
         }
@@ -493,7 +487,6 @@ __global__ __maxnreg__(48) void k_density_brick(const __grid_constant__ Phys P, 
     M.s_gidx = reinterpret_cast<int*>(M.sp + C.cap);
     M.s_off = M.s_gidx + C.cap;
     M.s_start = M.s_off + (G::R + 1);
-    M.s_cell = reinterpret_cast<unsigned short*>(M.s_start + G::R);
     M.s_list = reinterpret_cast<unsigned short*>(M.s_start);
     M.s_warp = s_warp;
     M.s_work = s_work;
@@ -858,10 +851,10 @@ Launch plan(const Phys& P, const Shape& s, int h) {
     // close to the mean), in whole warps, 64..512
     int t = (int)(s.bx * s.by * s.bz * ppc * 1.04 + 31) / 32 * 32;
     L.threads = t < 64 ? 64 : (t > 512 ? 512 : t);
-    // s_start (R ints) and s_cell (cap shorts) while staging; the drain queue after
+    // s_start (R ints) while staging; the drain queue after
     const size_t queue = (size_t)DLIST * L.threads * 2;
     auto smem_for = [&](size_t cap) {
-        const size_t start = (size_t)4 * R + 2 * cap;
+        const size_t start = (size_t)4 * R;
         return cap * 16 + cap * 4 + (size_t)4 * (R + 1) + ((queue > start ? queue : start) + 15) / 16 * 16;
     };
     // staging capacity: at least the expected region count times STAGE_MARGIN;
