@@ -428,7 +428,8 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
         // row's first cell; rows step by RX, planes by RX * RY) and tests one
         // candidate, with selects, so the lanes never diverge.  Lanes past
         // their last row (la >= la_end) see empty rows.  The warp votes once
-        // per 8 steps, so queues drain at DLIST - 8.
+        // per 4 steps, so queues drain at DLIST - 4 (drains run on fuller queues
+        // than with a vote per 8 steps, which matters most in clustered states).
         int la = 0, la_end = 0, cy = 0, k = 0, kend = 0;
         if (fast) {
             la = (zlo * G::RY + ly - STENCIL) * G::RX + lx - STENCIL;
@@ -437,7 +438,7 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
         }
         for (;;) {
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
+            for (int u = 0; u < 4; ++u) {
                 const bool adv = k >= kend;
                 int la2 = la + G::RX, cy2 = cy + 1;
                 const bool wrap = cy2 == 2 * STENCIL + 1;
@@ -459,7 +460,7 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
                     s_list[(n++) * T + threadIdx.x] = (unsigned short)k;
                 k += valid ? 1 : 0;
             }
-            if (__any_sync(0xffffffffu, n > DLIST - 8)) ASPH_DRAIN();
+            if (__any_sync(0xffffffffu, n > DLIST - 4)) ASPH_DRAIN();
             if (__all_sync(0xffffffffu, la >= la_end)) break;
         }
         ASPH_DRAIN();
