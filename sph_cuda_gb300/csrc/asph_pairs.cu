@@ -44,7 +44,7 @@
 namespace asph {
 
 constexpr int MAX_HALO = 3;      // widest staged halo (cells around a brick)
-constexpr int DLIST = 28;        // queued accepted candidates per thread (D)
+constexpr int DLIST = 30;        // queued accepted candidates per thread (D)
 constexpr int M_TPB = 256;
 constexpr int M_TPT = 2;         // targets per thread of the momentum pass
 
