@@ -725,14 +725,14 @@ __global__ __launch_bounds__(M_TPB, 4) void k_momentum(const __grid_constant__ P
                         for (; q + 4 <= cnt; q += 4) {
                             int jj[4];
                             float4 pp[4], vv[4];
-    #pragma unroll
+#pragma unroll
                             for (int u = 0; u < 4; ++u) jj[u] = A.nbr[(size_t)(q + u) * P.N + i];
-    #pragma unroll
+#pragma unroll
                             for (int u = 0; u < 4; ++u) {
                                 pp[u] = A.ms0[jj[u]];
                                 vv[u] = A.ms1[jj[u]];
                             }
-    #pragma unroll
+#pragma unroll
                             for (int u = 0; u < 4; ++u) msum_add(P, s, T, pp[u], vv[u]);
                         }
                         for (; q < cnt; ++q) {
