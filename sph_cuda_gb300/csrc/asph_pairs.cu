@@ -44,7 +44,7 @@
 namespace asph {
 
 constexpr int MAX_HALO = 3;      // widest staged halo (cells around a brick)
-constexpr int DLIST = 30;        // queued accepted candidates per thread (D)
+constexpr int DLIST = 30;        // most queued accepted candidates per thread (D); a launch may use fewer
 constexpr int M_TPB = 256;
 constexpr int M_TPT = 2;         // targets per thread of the momentum pass
 
@@ -79,6 +79,7 @@ struct BrickHalves {
 struct PairCfg {
     int nbx, nby, nbz, nbricks;
     int cap;            // staged particles that fit in shared memory
+    int dlist;          // drain-queue depth of this launch (<= DLIST; queues drain above dlist - 4)
 };
 
 namespace {
@@ -428,7 +429,7 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
         // row's first cell; rows step by RX, planes by RX * RY) and tests one
         // candidate, with selects, so the lanes never diverge.  Lanes past
         // their last row (la >= la_end) see empty rows.  The warp votes once
-        // per 4 steps, so queues drain at DLIST - 4 (drains run on fuller queues
+        // per 4 steps, so queues drain at dlist - 4 (drains run on fuller queues
         // than with a vote per 8 steps, which matters most in clustered states).
         int la = 0, la_end = 0, cy = 0, k = 0, kend = 0;
         if (fast) {
@@ -460,7 +461,7 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
                     s_list[(n++) * T + threadIdx.x] = (unsigned short)k;
                 k += valid ? 1 : 0;
             }
-            if (__any_sync(0xffffffffu, n > DLIST - 4)) ASPH_DRAIN();
+            if (__any_sync(0xffffffffu, n > C.dlist - 4)) ASPH_DRAIN();
             if (__all_sync(0xffffffffu, la >= la_end)) break;
         }
         ASPH_DRAIN();
@@ -853,32 +854,37 @@ Launch plan(const Phys& P, const Shape& s, int h) {
     int t = (int)(s.bx * s.by * s.bz * ppc * 1.04 + 31) / 32 * 32;
     L.threads = t < 64 ? 64 : (t > 512 ? 512 : t);
     // s_start (R ints) while staging; the drain queue after
-    const size_t queue = (size_t)DLIST * L.threads * 2;
-    auto smem_for = [&](size_t cap) {
-        const size_t start = (size_t)4 * R;
+    auto smem_for = [&](size_t cap, int dlist) {
+        const size_t queue = (size_t)dlist * L.threads * 2, start = (size_t)4 * R;
         return cap * 16 + cap * 4 + (size_t)4 * (R + 1) + ((queue > start ? queue : start) + 15) / 16 * 16;
     };
     // staging capacity: at least the expected region count times STAGE_MARGIN;
-    // beyond that, all the shared memory that the most resident blocks (as the
-    // registers allow) leave, so that clustered bricks overflow less often
-    // (an overflowing brick is split into halves)
+    // the most resident blocks the registers allow come first, then the
+    // deepest drain queue (fuller drains) that still fits them, then all the
+    // shared memory left for staging, so that clustered bricks overflow less
+    // often (an overflowing brick is split into halves)
     int need = (int)(R * ppc * STAGE_MARGIN) + 64;
     need = (need + 63) & ~63;
     need = need > MAX_STAGE ? MAX_STAGE : need;
     int per_sm, reserved;
     smem_limits(&per_sm, &reserved);
     const int by_regs = 65536 / (DENSITY_REGS * L.threads);
-    int cap = need;
-    for (int b = by_regs < 8 ? by_regs : 8; b >= 1; --b) {
+    int cap = need, dlist = 16;
+    bool found = false;
+    for (int b = by_regs < 8 ? by_regs : 8; b >= 1 && !found; --b) {
         const size_t budget = (size_t)(per_sm / b - reserved - 512);   // 512: the kernel's static arrays
-        if (smem_for(need) > budget) continue;
-        int c = MAX_STAGE;
-        while (c > need && smem_for(c) > budget) c -= 64;
-        cap = c;
-        break;
+        for (int d = DLIST; d >= 16 && !found; d -= 2) {
+            if (smem_for(need, d) > budget) continue;
+            int c = MAX_STAGE;
+            while (c > need && smem_for(c, d) > budget) c -= 64;
+            cap = c;
+            dlist = d;
+            found = true;
+        }
     }
     L.C.cap = cap;
-    L.smem = smem_for(cap);
+    L.C.dlist = dlist;
+    L.smem = smem_for(cap, dlist);
     return L;
 }
 
