@@ -44,6 +44,7 @@
 namespace asph {
 
 constexpr int MAX_HALO = 3;      // widest staged halo (cells around a brick)
+constexpr int DENSITY_REGS = 48; // register cap of the brick kernel (its launch plan counts on it)
 constexpr int DLIST = 30;        // most queued accepted candidates per thread (D); a launch may use fewer
 constexpr int M_TPB = 256;
 constexpr int M_TPT = 2;         // targets per thread of the momentum pass
@@ -473,10 +474,10 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
     }
 }
 
-// 48 registers keep 4 blocks of up to 320 threads per SM (the shared-memory
-// limit at the default staging capacity).
+// DENSITY_REGS = 48 registers keep 4 blocks of up to 320 threads per SM (the
+// shared-memory limit at the default staging capacity).
 template <int BX, int BY, int BZ, int H>
-__global__ __maxnreg__(48) void k_density_brick(const __grid_constant__ Phys P, const __grid_constant__ DArgs A,
+__global__ __maxnreg__(DENSITY_REGS) void k_density_brick(const __grid_constant__ Phys P, const __grid_constant__ DArgs A,
                                                        PairCfg C) {
     using G = BrickGeom<BX, BY, BZ, H>;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -839,7 +840,6 @@ void smem_limits(int* per_sm, int* reserved) {
     *reserved = res;
 }
 
-constexpr int DENSITY_REGS = 48;   // the brick kernel's register cap (__maxnreg__)
 
 Launch plan(const Phys& P, const Shape& s, int h) {
     Launch L;
