@@ -4,7 +4,7 @@ reference's own kernels.
 Bit-exact: Morton keys, the sorted permutation, sorted keys, cell table,
 surface list, gathered fields.  Floating point: single-stage results agree
 with the FP64 oracle to a normwise relative error of 1e-5
-(||gpu - oracle||_inf / ||oracle||_inf per field), the benchmark spec's bound.
+(||gpu - oracle||_inf / ||oracle||_inf per field), the single-step bound.
 Each stage of the oracle is fed the GPU's own output of the previous stage,
 so that both sides search identical cell windows.
 """

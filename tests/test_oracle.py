@@ -12,7 +12,7 @@ from oracle import oracle
 from sph_cuda_gb300 import preset
 from conftest import golden, normwise
 
-TOL = 1e-5          # normwise single-step tolerance (the benchmark spec)
+TOL = 1e-5          # normwise single-step tolerance
 
 
 def test_helpers_match_reference_host_code():
