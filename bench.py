@@ -8,9 +8,11 @@ re-sort every step).  Synthetic, seeded initial state; no dataset.
 
 ours: K fused steps (sort + gather/kick/drift/flux + density/EOS/micro +
 momentum/integrate/rain/CFL, one CUDA graph per step) timed with CUDA events
-on the simulation stream; one JSON line on rank 0.  --impl reference times
-the CPU restatement of the reference (FP64, all host cores) on a bounded
-sample of the same workload.
+on the simulation stream; one JSON line on rank 0.  Beside it: the per-kernel
+times over the same K states, the reference's own kernels on this GPU
+(`reference_gpu`) and the FP64 CPU port (`cpu_baseline`), both from the same
+initial state.  --impl reference times the CPU restatement of the reference
+(FP64, all host cores) on the full configuration.
 """
 from __future__ import annotations
 
@@ -123,33 +125,23 @@ def dist_setup():
     return ws, rank, local
 
 
-def cpu_sample_params():
-    """The moist-bubble physics on a quarter-width box: 32 x 32 x 128 lattice (131,072
-    particles), 33 x 33 x 200 cells of the same 150.4 x 150.4 x 40 m size, so
-    the per-particle neighbour work equals the full workload's."""
-    import sph_cuda_gb300 as sph
-    p = sph.preset("bubble2m")
-    p.nx = p.ny = 33
-    p.lat_nx = p.lat_ny = 32
-    p.n_particles = 32 * 32 * 128
-    for b in range(p.n_bubbles):
-        p.bubble_x[b] *= 33 / 133.0
-        p.bubble_y[b] *= 33 / 133.0
-    return p
-
-
-def time_oracle(p, state, nsteps: int):
+def oracle_timed(p, warmup: int, steps: int = 0, budget_s: float = 12.0):
+    """FP64 oracle steps (all host threads) of the full configuration, from
+    the state the library's init leaves (restated by the oracle): `warmup`
+    untimed steps, then `steps` timed steps, or, with steps = 0, as many as
+    fill about `budget_s` seconds.  Returns (seconds, steps, threads)."""
     from oracle import oracle
+    s = oracle.initial_state(p)
+    rain = s["rain"]
+    st, rg, pr, ctl, _ = oracle.run(p, s, max(warmup, 1), rain)
+    if steps <= 0:
+        t0 = time.perf_counter()
+        st, rg, pr, ctl, _ = oracle.run(p, st, 1, rg, pr, ctl)
+        t1 = time.perf_counter() - t0
+        steps = int(min(400, max(3, round(budget_s / max(t1, 1e-3)))))
     t0 = time.perf_counter()
-    _, _, _, ctl, st = oracle.run(p, state, nsteps)
-    dt = time.perf_counter() - t0
-    return dt, oracle.threads(), st
-
-
-def oracle_initial_state(p):
-    """Initial state of the CPU runs from the oracle's own init."""
-    from oracle import oracle
-    return oracle.init_state(p)
+    oracle.run(p, st, steps, rg, pr, ctl)
+    return time.perf_counter() - t0, steps, oracle.threads()
 
 
 def workload_string(name: str) -> str:
@@ -166,32 +158,87 @@ def metric_for(p) -> str:
 
 
 def run_reference(args):
-    """The reference's CPU path (the FP64 oracle port, all host threads) on a
-    bounded sample of the workload: each step is one full step of the
-    131,072-particle box with the workload's cells and physics."""
+    """The reference's CPU path: the FP64 oracle port (the reference has no
+    CPU implementation of its step) with all host threads, on the full
+    configuration of the workload: init, W warm-up steps, K timed steps.
+    Parameters come from the oracle's own preset table, so this arm neither
+    imports the product package nor loads the CUDA library."""
     ws, rank, local = dist_setup()
     if rank != 0:
         return 0
-    from oracle import oracle
-    p = cpu_sample_params()
-    state = oracle_initial_state(p)
-    oracle.run(p, state, max(args.warmup, 1))   # warm-up: page in, thread pool
-    t, cores, _ = time_oracle(p, state, args.steps)
-    value = p.n_particles * args.steps / t
-    sample = ("%d consecutive FP64 steps of the 131,072-particle moist-bubble box "
-              "(same cells and physics, 5 x 5 km footprint)" % args.steps)
+    from oracle import params
+    if args.workload not in ("bubble2m", "bubble524k", "reference128", "large16m"):
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no form of the %s workload"
+                          % args.workload}))
+        return 0
+    p = params.workload(args.workload)
+    t, steps, cores = oracle_timed(p, args.warmup, args.steps)
+    value = p.n_particles * steps / t
+    sample = ("the full configuration (%d particles, %d cells): %d FP64 steps after init and %d warm-up steps"
+              % (p.n_particles, p.nx * p.ny * p.nz, steps, max(args.warmup, 1)))
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "impl": "reference", "metric": metric_for(p), "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": workload_string(args.workload), "sample": sample,
-                   "sample_particles": p.n_particles, "sample_cells": p.nx * p.ny * p.nz},
+        "config": {"workload": workload_string(args.workload), "particles": p.n_particles,
+                   "cells": p.nx * p.ny * p.nz},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
+
+
+def reference_gpu(args, ours_value: float):
+    """The reference's own kernels (asph_h100.cu compiled for sm_103a with
+    the workload's cell sizes) in its host step loop on this GPU, from the
+    same initial state, W untimed steps then K timed: the comparator of the
+    plain step.  Runs after our timed region, in a child process."""
+    if args.workload not in ("bubble2m", "reference128"):
+        return None
+    script = os.path.join(ROOT, "oracle", "time_reference.py")
+    mode = "bubble2m" if args.workload == "bubble2m" else "native"
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    try:
+        r = subprocess.run([sys.executable, script, mode, str(args.steps), str(max(args.warmup, 1))],
+                           capture_output=True, text=True, timeout=900)
+    except Exception as e:   # the harness is test infrastructure: report, do not fail the bench
+        clocks.stop()
+        return {"unavailable": "reference kernels did not run: %s" % str(e).splitlines()[0]}
+    clk = clocks.stop()
+    line = None
+    for ln in r.stdout.splitlines():
+        if ln.startswith("{") and "reference-gpu" in ln:
+            line = json.loads(ln)
+    if r.returncode != 0 or line is None:
+        tail = (r.stderr or r.stdout or "").strip().splitlines()[-1:] or ["no output"]
+        return {"unavailable": "reference kernels exited %d: %s" % (r.returncode, tail[0])}
+    return {"ms_per_step": line["ms_per_step"], "particle_steps_per_s": line["particle_steps_per_s"],
+            "steps": line["steps"], "warmup": line.get("warmup"), "speedup": ours_value / line["particle_steps_per_s"],
+            "how": "asph_h100.cu's kernels (cubin built from the reference source with its own flags, cell sizes "
+                   "of the workload) in its step loop: CUB sort every step, host CFL read-back per step",
+            "clocks": clk}
+
+
+def traffic_record(workload: str, steps_before: int, kernel: str):
+    """DRAM bytes of one launch of `kernel` captured by ncu in exactly the
+    state the line's per-kernel times cover: profiles/traffic_<workload>.json
+    holds captures keyed by the number of steps completed before the captured
+    launch.  No capture for this state: None (the line says so)."""
+    path = os.path.join(ROOT, "profiles", "traffic_%s.json" % workload)
+    if not os.path.exists(path):
+        return None
+    try:
+        d = json.load(open(path))
+    except Exception:
+        return None
+    for rec in d.get("captures", []):
+        if rec.get("steps_before") == steps_before and kernel in rec.get("bytes", {}):
+            return {"bytes": rec["bytes"][kernel], "source": d.get("source", path), "command": rec.get("command"),
+                    "companion": rec.get("companion", {}).get(kernel)}
+    return None
 
 
 def workload_params(name: str):
@@ -239,6 +286,8 @@ def run_ours(args):
         sim.step(args.advance)
     sim.step(max(args.warmup, 1))
     per_step = sim.step_kernels()   # kernel nodes of the step's CUDA graph
+    steps_before = int(sim.control()["step"])   # steps completed when the timed region starts
+    start = sim.snapshot()          # the timed region's first state, replayed for the per-kernel times
 
     def barrier():
         if dist is not None:
@@ -259,35 +308,23 @@ def run_ours(args):
     barrier()
     value, sec = job_rate(N * args.steps, e0.elapsed_time(e1) / 1e3, dist, "cuda")
     ms = sec * 1e3
+    ctl = sim.control()
 
-    # per-kernel device times of the same step (non-graph launches, events
-    # between the kernels on the simulation stream)
-    prof_steps = max(3, min(args.steps, 20))
-    ph = sim.step_profiled(prof_steps)
-    ph_ms = {k: v / prof_steps for k, v in ph.items()}
+    # per-kernel device times over the very states of the timed region: the
+    # same K steps again from the snapshot (results are deterministic), with
+    # events between the phases on the simulation stream
+    sim.restore(start)
+    ph = sim.step_profiled(args.steps)
+    ph_ms = {k: v / args.steps for k, v in ph.items()}
+    start.close()
     algo = algorithmic_bytes(N, C)
     kernels = ["table_clear", "sort", "gather_kick_drift", "density_eos", "momentum_integrate"]
     dom = max(kernels, key=lambda k: ph_ms[k])
     hbm, src = peaks()
     achieved = algo[dom] / (ph_ms[dom] / 1e3) / 1e9
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic_%s.txt" % args.workload)
-    if os.path.exists(tfile):
-        try:
-            traffic = json.load(open(tfile)).get(dom)
-        except Exception:
-            traffic = None
-    # the pair kernels are bound by instruction issue and load latency, not
-    # HBM: their pipe utilisation from the committed ncu capture goes beside
-    # the HBM fraction
-    companion = None
-    pfile = os.path.join(ROOT, "profiles", "pipes_bubble2m.txt")
-    if os.path.exists(pfile):
-        try:
-            d = json.load(open(pfile))
-            companion = dict(d.get(dom, {}), source=d.get("source"))
-        except Exception:
-            companion = None
+    # DRAM traffic of the dominant kernel from an ncu capture of the first
+    # timed step of this same command (profiles/traffic_<workload>.json)
+    trec = traffic_record(args.workload, steps_before, dom)
 
     # end to end through the C ABI with pinned host buffers: per step the
     # persistent state goes host->device, one step runs, the state comes back
@@ -303,21 +340,18 @@ def run_ours(args):
         sim.get_state(fields, out=host)
     e2e, _ = job_rate(N * e2e_steps, time.perf_counter() - t0, dist, "cuda")
     nbytes = len(fields) * 4 * N
+    sim.close()
 
-    cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu and args.workload == "bubble2m":
-        ps = cpu_sample_params()
-        st = oracle_initial_state(ps)
-        nsteps = args.cpu_steps
-        if nsteps <= 0:   # size the sample to about 12 s of CPU work
-            t1, _, _ = time_oracle(ps, st, 1)
-            nsteps = int(min(400, max(3, round(12.0 / max(t1, 1e-3)))))
-        tc, cores, _ = time_oracle(ps, st, nsteps)
-        cpu = {"value": ps.n_particles * nsteps / tc, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": "%d consecutive FP64 steps of the 131,072-particle moist-bubble box "
-                         "(same cells and physics, 5 x 5 km footprint) in %.1f s" % (nsteps, tc)}
+    cpu, ref_gpu = None, None
+    if rank == 0 and ws == 1:
+        if not args.no_reference_gpu:
+            ref_gpu = reference_gpu(args, value)
+        if not args.no_cpu:
+            tc, nsteps, cores = oracle_timed(p, args.warmup, args.cpu_steps)
+            cpu = {"value": N * nsteps / tc, "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": "%d FP64 steps of the full configuration after init and %d warm-up steps, in %.1f s"
+                             % (nsteps, max(args.warmup, 1), tc)}
 
-    ctl = sim.control()
     if rank == 0:
         line = {
             "metric": metric_for(p), "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -325,14 +359,21 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload_string(args.workload),
                        "particles": N, "cells": C, "dt_s": ctl["dt"], "advance_steps": args.advance,
+                       "steps_before_timed": steps_before,
                        "l2": "working set %.0f MB > 129 MB L2 (no flush needed)" % ((N * 164 + C * 20) / 1e6),
                        "parallelism": "replicas x%d" % ws},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
-                         "companion": companion,
-                         "step_achieved": algo["step"] / (ph_ms["step"] / 1e3) / 1e9,
-                         "kernel_ms": ph_ms},
+                         "frac": achieved / hbm, "peak_source": src,
+                         "traffic": None if trec is None else trec["bytes"],
+                         "traffic_source": ("no ncu capture of step %d of this workload" % (steps_before + 1))
+                         if trec is None else trec["source"],
+                         "companion": None if trec is None else trec["companion"],
+                         "kernel_ms": ph_ms, "kernel_ms_over": "the timed region's %d steps, replayed from a "
+                                                               "snapshot with events between phases" % args.steps,
+                         "frac_step": algo["step"] / N * (value / ws) / 1e9 / hbm,
+                         "step_bytes_per_particle": algo["step"] / N},
             "cpu_baseline": cpu,
+            "reference_gpu": ref_gpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "steps": e2e_steps, "api": "asph_set_state + asph_step(1) + asph_get_state, pinned host SoA"},
             "gpu_launches": per_step * args.steps,
@@ -341,7 +382,6 @@ def run_ours(args):
                       "wmax": ctl["wmax"], "deferred_targets_last_step": ctl["deferred"]},
         }
         print(json.dumps(line))
-    sim.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0
@@ -476,6 +516,7 @@ def parse_args(argv=None):
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=0, help="0: about 12 s of oracle steps")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true", help="skip the reference-kernel comparator")
     ap.add_argument("--advance", type=int, default=0,
                     help="untimed steps after init, before warm-up (profile a developed state)")
     ap.add_argument("--workload", default="bubble2m",

@@ -232,18 +232,27 @@ static double normal01(uint32_t seed, uint32_t i, uint32_t stream) {
 }
 
 /* Jittered-lattice init with Gaussian warm bubbles and Gaussian theta noise
- * (no counterpart in the reference, which only has the cell-centre lattice). */
+ * (no counterpart in the reference, which only has the cell-centre lattice).
+ * Positions are float32 values formed by the float operations the library's
+ * init uses, each rounded once (this file is built without FMA contraction),
+ * so they, and the keys derived from them, match bit for bit; the profiles
+ * are evaluated in double at those positions. */
+static double lattice_coord(int i, float jitter, uint32_t seed, uint32_t i_part, uint32_t stream, float s) {
+    float j = jitter * (float)(2.0 * uniform24(seed, i_part, stream) - 1.0);   /* 2u - 1 is exact */
+    float c = ((float)i + 0.5f) + j;
+    return (double)(c * s);
+}
 int or_init_lattice(const AsphParams* p, double* x, double* y, double* z, double* th, double* qv, double* rho) {
     OP o; derive(p, &o);
     const int lnx = p->lat_nx, lny = p->lat_ny, lnz = p->lat_nz;
     if ((long long)lnx * lny * lnz != o.N) return ASPH_ERR_CONFIG;
+    const float sx = (float)o.lx / (float)lnx, sy = (float)o.ly / (float)lny, sz = (float)o.lz / (float)lnz;
     #pragma omp parallel for schedule(static)
     for (int i = 0; i < o.N; ++i) {
         int ix = i % lnx, iy = (i / lnx) % lny, iz = i / (lnx * lny);
-        double sx = o.lx / lnx, sy = o.ly / lny, sz = o.lz / lnz;
-        double px = (ix + 0.5 + p->jitter * (2.0 * uniform24(p->seed, (uint32_t)i, 0u) - 1.0)) * sx;
-        double py = (iy + 0.5 + p->jitter * (2.0 * uniform24(p->seed, (uint32_t)i, 1u) - 1.0)) * sy;
-        double pz = (iz + 0.5 + p->jitter * (2.0 * uniform24(p->seed, (uint32_t)i, 2u) - 1.0)) * sz;
+        double px = lattice_coord(ix, p->jitter, p->seed, (uint32_t)i, 0u, sx);
+        double py = lattice_coord(iy, p->jitter, p->seed, (uint32_t)i, 1u, sy);
+        double pz = lattice_coord(iz, p->jitter, p->seed, (uint32_t)i, 2u, sz);
         double t = theta_ref(&o, pz);
         for (int b = 0; b < p->n_bubbles; ++b) {
             double dx = px - p->bubble_x[b], dy = py - p->bubble_y[b], dz = pz - p->bubble_z[b];
@@ -632,6 +641,98 @@ int or_hash_noise(int n, const int* ijk, float* out) {
     for (int i = 0; i < n; ++i) out[i] = hash_noise(ijk[3 * i], ijk[3 * i + 1], ijk[3 * i + 2]);
     return 0;
 }
+/* ========================================================================= */
+/* Parameter presets, restated on the oracle side so that the CPU legs of    */
+/* the benchmark never load the CUDA library.  Same float expressions as the */
+/* library's table (include/asph.h ASPH_PRESET_*); a CPU test holds the two  */
+/* equal field by field.  The reference physics are asph_h100.cu:48-120.    */
+/* ========================================================================= */
+static float preset_uniform(uint32_t i, uint32_t stream) {
+    uint64_t h = mix64(((uint64_t)1u << 32) ^ mix64(((uint64_t)stream << 40) ^ (uint64_t)i));
+    return (float)(uint32_t)(h >> 40) * (1.0f / 16777216.0f);
+}
+static void preset_reference_physics(AsphParams* p) {
+    p->dx = 1000.0f; p->dy = 1000.0f; p->dz = 100.0f;            /* asph_h100.cu:48 */
+    p->th0 = 300.0f; p->n2 = 6.0e-5f; p->cs = 80.0f;              /* asph_h100.cu:71-73 */
+    p->qv_mode = ASPH_QV_REFERENCE; p->qv0 = 0.016f; p->rh = 0.8f; p->rh_bl = 0.8f; p->z_bl = 0.f;
+    p->alpha_av = 0.2f; p->beta_av = 0.0f; p->h_av = 0.f;         /* asph_h100.cu:84-85 */
+    p->sponge_sigma = 0.05f; p->sponge_frac = 0.15f; p->dthdt_cap = 1.0f;   /* asph_h100.cu:89-91 */
+    p->surface_flux = 1;
+    p->c_h = 1.2e-3f; p->c_e = 1.2e-3f; p->beta_moist = 0.20f; p->v_bg = 7.0f; p->dts_skin = 3.15f;
+    p->ramp = 3600.0f;                                             /* asph_h100.cu:100-105 */
+    p->qc_auto = 1.0e-3f; p->rate_auto = 1.0e-3f; p->v_rain = 9.0f; p->theta_cap = 500.0f;
+    p->qv_cap = 0.060f;                                            /* asph_h100.cu:111-120 */
+    p->accretion = 0; p->rain_evap = 0; p->k_accr = 2.2f;
+    p->dt_request = 0.f; p->cfl = 0.40f; p->max_trip = 20; p->strict_cfl = 0; p->adaptive_dt = 1;
+    p->sort_every = 0; p->permute_acc = 0; p->pmass = 0.f;
+    p->dump_sx = 10; p->dump_sy = 10; p->dump_sz = 3;             /* asph_h100.cu:737 */
+    p->init_mode = ASPH_INIT_REFERENCE; p->noise = 0.1f; p->seed = 0; p->jitter = 0.f;
+}
+static void preset_config_physics(AsphParams* p, float Lx, float Ly, float Lz, float hxy, float hz, int lnx,
+                                  int lny, int lnz) {
+    preset_reference_physics(p);
+    p->nx = (int)floorf(Lx / hxy); p->ny = (int)floorf(Ly / hxy); p->nz = (int)floorf(Lz / hz);
+    p->dx = Lx / p->nx; p->dy = Ly / p->ny; p->dz = Lz / p->nz;
+    p->n2 = 9.80665f * 4.0e-3f / 300.0f;                           /* 4 K/km at the surface */
+    p->qv_mode = ASPH_QV_RH; p->rh = 0.8f; p->rh_bl = 0.8f; p->z_bl = 0.f;
+    p->accretion = 1; p->rain_evap = 1;
+    p->permute_acc = 1;
+    p->init_mode = ASPH_INIT_LATTICE;
+    p->lat_nx = lnx; p->lat_ny = lny; p->lat_nz = lnz;
+    p->n_particles = lnx * lny * lnz;
+    p->jitter = 0.25f; p->seed = 0; p->noise = 0.f;
+}
+int or_params_preset(AsphParams* p, int preset, int nx, int ny, int nz) {
+    memset(p, 0, sizeof(*p));
+    switch (preset) {
+        case ASPH_PRESET_REFERENCE:
+            preset_reference_physics(p);
+            p->nx = 1000; p->ny = 1000; p->nz = 150;              /* asph_h100.cu:729 */
+            if (nx > 0) p->nx = nx;
+            if (ny > 0) p->ny = ny;
+            if (nz > 0) p->nz = nz;
+            p->n_particles = p->nx * p->ny * p->nz;
+            return 0;
+        case ASPH_PRESET_SMALL_65K:
+        case ASPH_PRESET_ADJOINT_262K: {
+            const int n = preset == ASPH_PRESET_SMALL_65K ? 32 : 64;
+            preset_config_physics(p, 10000.f, 10000.f, 5000.f, 200.f, 50.f, n, n, 64);
+            p->n_bubbles = 1;
+            p->bubble_x[0] = 5000.f; p->bubble_y[0] = 5000.f; p->bubble_z[0] = 1000.f;
+            p->bubble_r[0] = 1000.f; p->bubble_amp[0] = 2.0f;
+            p->dt_request = 0.5f;
+            p->sort_every = 0;
+            break;
+        }
+        case ASPH_PRESET_BUBBLE_2M:
+            preset_config_physics(p, 20000.f, 20000.f, 8000.f, 150.f, 40.f, 128, 128, 128);
+            p->n_bubbles = 3;
+            for (int b = 0; b < 3; ++b) {
+                p->bubble_x[b] = 20000.f * (0.2f + 0.6f * preset_uniform((uint32_t)b, 10u));
+                p->bubble_y[b] = 20000.f * (0.2f + 0.6f * preset_uniform((uint32_t)b, 11u));
+                p->bubble_z[b] = 800.f + 800.f * preset_uniform((uint32_t)b, 12u);
+                p->bubble_r[b] = 800.f + 700.f * preset_uniform((uint32_t)b, 13u);
+                p->bubble_amp[b] = 1.5f + 1.5f * preset_uniform((uint32_t)b, 14u);
+            }
+            p->dt_request = 0.25f;
+            p->sort_every = 1;
+            break;
+        case ASPH_PRESET_LARGE_16M:
+            preset_config_physics(p, 40000.f, 40000.f, 10000.f, 160.f, 20.f, 256, 256, 256);
+            p->rh_bl = 0.95f; p->z_bl = 1000.f;
+            p->noise = 0.2f;
+            p->dt_request = 0.f;
+            p->sort_every = 1;
+            break;
+        default:
+            return ASPH_ERR_ARG;
+    }
+    if (nx > 0) p->nx = nx;
+    if (ny > 0) p->ny = ny;
+    if (nz > 0) p->nz = nz;
+    return 0;
+}
+
 int or_derived(const AsphParams* p, double out[12]) {
     OP o; derive(p, &o);
     out[0] = o.pmass; out[1] = o.mm; out[2] = o.dt_static; out[3] = o.dt_cap; out[4] = o.dt_floor;

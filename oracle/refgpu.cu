@@ -15,7 +15,7 @@
 //   refgpu <cubin> init <nx> <ny> <nz> <noise> <outdir>
 //   refgpu <cubin> run <nx> <ny> <nz> <steps> <dt> <sort_every>
 //          sort_every 0 = the reference's displacement-gated cadence
-//   refgpu <cubin> runstate <in.bin> <steps> <dx> <dy> <dz>
+//   refgpu <cubin> runstate <in.bin> <steps> <warmup> <dx> <dy> <dz>
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
@@ -361,10 +361,12 @@ static int cmd_run(const Ref& R, int nx, int ny, int nz, int steps, float dt_req
 }
 
 // The reference step loop on a given state (cmd_stages input format), a sort
-// every step, for timing: K steps at the state's dt with the reference's
-// per-step velocity maxima read back to the host (asph_h100.cu:1043-1046).
-// Cell sizes are passed because the cubin may carry other constexprs.
-static int cmd_runstate(const Ref& R, const char* in, int steps, float dx, float dy, float dz) {
+// every step, for timing: `warmup` untimed steps, then K timed steps, each
+// with the reference's per-step velocity maxima read back to the host and
+// its closed-loop dt control (asph_h100.cu:1040-1073), starting from the
+// state's dt.  Cell sizes are passed because the cubin may carry other
+// constexprs.
+static int cmd_runstate(const Ref& R, const char* in, int steps, int warmup, float dx, float dy, float dz) {
     FILE* f = fopen(in, "rb");
     if (!f) { fprintf(stderr, "cannot open %s\n", in); return 1; }
     int32_t hdr[8];
@@ -379,6 +381,8 @@ static int cmd_runstate(const Ref& R, const char* in, int steps, float dx, float
     fclose(f);
     launch(R.iota, bpb(d.N), TPB, d.valsIn, d.N);
     const float Lx = d.nx * dx, Ly = d.ny * dy, Lz = d.nz * dz;
+    const float dt_cap = dt, dt_floor = 0.05f * dt_cap;
+    int trips = 0;
     float hg[3];
     auto now = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
     auto one = [&]() {
@@ -406,16 +410,27 @@ static int cmd_runstate(const Ref& R, const char* in, int steps, float dx, float
         CK(cudaMemsetAsync(d.gmax, 0, 12));
         launch(R.maxvel, 1024, TPB, (const float4*)d.vel, d.N, d.gmax);
         CK(cudaMemcpy(hg, d.gmax, 12, cudaMemcpyDeviceToHost));
+        const float req = 0.40f * fminf(fminf(dx / (CS + hg[0]), dy / (CS + hg[1])), dz / (CS + hg[2])) * 0.90f;
+        float adopt = fminf(dt_cap, req);
+        if (adopt < dt_floor) {
+            ++trips;
+            launch(R.clampv, 1024, TPB, d.vel, d.N, 0.5f * CS);
+            adopt = fmaxf(dt_floor, 0.40f * fminf(fminf(dx, dy), dz) / (1.5f * CS) * 0.90f);
+        } else if (adopt < 0.98f * dt) {
+            trips = 0;
+        }
+        dt = adopt;
     };
-    for (int k = 0; k < 3; ++k) one();   // warm-up
+    for (int k = 0; k < warmup; ++k) one();
     CK(cudaDeviceSynchronize());
     const double t0 = now();
     for (int k = 0; k < steps; ++k) one();
     CK(cudaDeviceSynchronize());
     const double wall = now() - t0;
-    printf("{\"impl\": \"reference-gpu\", \"N\": %d, \"cells\": %d, \"steps\": %d, \"wall_s\": %.6f, "
-           "\"particle_steps_per_s\": %.6e, \"ms_per_step\": %.6f, \"wmax\": %.4f}\n",
-           d.N, d.C, steps, wall, (double)d.N * steps / wall, 1e3 * wall / steps, hg[2]);
+    printf("{\"impl\": \"reference-gpu\", \"N\": %d, \"cells\": %d, \"steps\": %d, \"warmup\": %d, "
+           "\"wall_s\": %.6f, \"particle_steps_per_s\": %.6e, \"ms_per_step\": %.6f, \"wmax\": %.4f, "
+           "\"final_dt\": %.6f, \"trips\": %d}\n",
+           d.N, d.C, steps, warmup, wall, (double)d.N * steps / wall, 1e3 * wall / steps, hg[2], dt, trips);
     return 0;
 }
 
@@ -433,9 +448,9 @@ int main(int argc, char** argv) {
     if (cmd == "run" && argc == 9)
         return cmd_run(R, atoi(argv[3]), atoi(argv[4]), atoi(argv[5]), atoi(argv[6]), (float)atof(argv[7]),
                        atoi(argv[8]));
-    if (cmd == "runstate" && argc == 8)
-        return cmd_runstate(R, argv[3], atoi(argv[4]), (float)atof(argv[5]), (float)atof(argv[6]),
-                            (float)atof(argv[7]));
+    if (cmd == "runstate" && argc == 9)
+        return cmd_runstate(R, argv[3], atoi(argv[4]), atoi(argv[5]), (float)atof(argv[6]), (float)atof(argv[7]),
+                            (float)atof(argv[8]));
     fprintf(stderr, "bad arguments\n");
     return 1;
 }

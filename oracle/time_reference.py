@@ -1,14 +1,16 @@
 """Time the reference's own kernels on the GPU (test infrastructure only).
 
-  python oracle/time_reference.py native   [steps]   reference geometry 128^3, its own init
-  python oracle/time_reference.py bubble2m [steps]   the 2,097,152-particle moist-bubble state
+  python oracle/time_reference.py native   [steps]            reference geometry 128^3, its own init
+  python oracle/time_reference.py bubble2m [steps] [warmup]   the 2,097,152-particle moist-bubble state
 
 `native` runs the unmodified reference cubin with the reference's own init
 and step loop, a sort every step.  `bubble2m` runs the reference's kernels
 compiled with the moist-bubble cell sizes (oracle/build_oracle.py) on the
 moist-bubble initial state restated by the oracle (jittered 128^3 lattice,
-three bubbles), a sort every step, dt = 0.2 s (the reference's static CFL
-bound for 40 m cells).  Prints the refgpu JSON line.
+three bubbles, initial sort and forces), a sort every step, starting at
+dt = 0.2 s (the reference's static CFL bound for 40 m cells) under the
+reference's closed-loop dt control: `warmup` untimed steps, then `steps`
+timed ones.  Prints the refgpu JSON line.
 """
 from __future__ import annotations
 
@@ -46,16 +48,18 @@ def write_state(path: str, p, s: dict, dt: float, simt: float = 0.0) -> None:
 def main() -> int:
     mode = sys.argv[1] if len(sys.argv) > 1 else "bubble2m"
     steps = int(sys.argv[2]) if len(sys.argv) > 2 else 50
+    warmup = int(sys.argv[3]) if len(sys.argv) > 3 else 3
     exe = build_oracle.build_refgpu()
     if mode == "native":
         return subprocess.call([exe, build_oracle.CUBIN, "run", "128", "128", "128", str(steps), "0.25", "1"])
-    import sph_cuda_gb300 as sph
-    p = sph.preset("bubble2m")
-    s = oracle.init_state(p)
+    from oracle import params
+    p = params.preset("bubble2m")
+    s = oracle.initial_state(p)
+    dt = float(np.float32(oracle.derived(p)["dt_cap"]))
     with tempfile.TemporaryDirectory() as td:
         path = os.path.join(td, "state.bin")
-        write_state(path, p, s, 0.2)
-        return subprocess.call([exe, build_oracle.BUBBLE2M_CUBIN, "runstate", path, str(steps),
+        write_state(path, p, s, dt)
+        return subprocess.call([exe, build_oracle.BUBBLE2M_CUBIN, "runstate", path, str(steps), str(warmup),
                                 repr(float(p.dx)), repr(float(p.dy)), repr(float(p.dz))])
 
 

@@ -178,6 +178,18 @@ extern "C" int asph_params_check(const AsphParams* p) {
     return ASPH_OK;
 }
 
+AuditConst asph::audit_constants(const AsphParams& p) {
+    AuditConst A;
+    A.th0 = p.th0;
+    A.n2 = p.n2;
+    A.a_exner = 9.80665 * 9.80665 / (1004.0 * A.th0 * A.n2);
+    const double lx = (double)((float)p.nx * p.dx), ly = (double)((float)p.ny * p.dy),
+                 lz = (double)((float)p.nz * p.dz);
+    A.pmass = p.pmass > 0.f ? (double)p.pmass : 100000.0 / (287.05 * A.th0) * lx * ly * lz / (double)p.n_particles;
+    A.N = p.n_particles;
+    return A;
+}
+
 static void derive(const AsphParams& p, Phys& P) {
     memset(&P, 0, sizeof(P));
     P.nx = p.nx; P.ny = p.ny; P.nz = p.nz; P.nxy = p.nx * p.ny;
@@ -995,7 +1007,7 @@ extern "C" int asph_audit(asph_ctx* c, double out[6]) {
         CKR(c->alloc(&c->audit_out, 6 * sizeof(double)));
     }
     apply_pending_clamp(c);
-    launch_audit(c->P, c->B, c->audit_part, c->audit_blocks, c->audit_out, c->stream);
+    launch_audit(c->P, audit_constants(c->prm), c->B, c->audit_part, c->audit_blocks, c->audit_out, c->stream);
     CKR(cudaGetLastError());
     CKR(cudaMemcpyAsync(out, c->audit_out, 6 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CKR(cudaStreamSynchronize(c->stream));

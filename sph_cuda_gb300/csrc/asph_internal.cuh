@@ -133,7 +133,17 @@ int pair_shape_count();
 bool pair_shape_fits(const Phys& P, int k);
 void launch_cfl(const Phys& P, const Bufs& B, cudaStream_t s);
 void launch_clamp(const Phys& P, const Bufs& B, cudaStream_t s);
-void launch_audit(const Phys& P, const Bufs& B, double* partial, int nblk, double* out, cudaStream_t s);
+// FP64 constants of the conservation audit, evaluated on the host in double
+// from the float parameters: the Exner coefficient g^2/(cp th0 N^2)
+// (asph_h100.cu:140) and the particle mass rho0 Lx Ly Lz / N
+// (asph_h100.cu:75-76 for one particle per cell), unless a mass is given.
+struct AuditConst {
+    double th0, n2, a_exner, pmass;
+    int N;
+};
+AuditConst audit_constants(const AsphParams& p);
+void launch_audit(const Phys& P, const AuditConst& A, const Bufs& B, double* partial, int nblk, double* out,
+                  cudaStream_t s);
 void launch_surf_flags(const Phys& P, const Bufs& B, uint8_t* flags, cudaStream_t s);
 void launch_coarse(const Phys& P, const Bufs& B, float* out, int sx, int sy, int sz, int cx, int cy,
                    int cz, float4* coldiag, cudaStream_t s);

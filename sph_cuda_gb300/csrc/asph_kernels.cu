@@ -38,13 +38,16 @@ __global__ void k_init(const __grid_constant__ Phys P, const __grid_constant__ I
         qv = fmaxf(qv_ref(P, z) * (1.0f + 0.02f * hash_noise(ix + 17, iy + 31, iz + 7)), 0.f);
     } else {
         const int ix = i % A.lnx, iy = (i / A.lnx) % A.lny, iz = i / (A.lnx * A.lny);
+        // Positions use explicitly rounded float operations (no contraction
+        // into FMAs), so that a host restatement in float reproduces them,
+        // and with them the Morton keys, bit for bit.  2u - 1 is exact.
         const float sx = P.lx / A.lnx, sy = P.ly / A.lny, sz = P.lz / A.lnz;
-        const float jx = A.jitter * (2.f * uniform24(A.seed, (uint32_t)i, 0u) - 1.f);
-        const float jy = A.jitter * (2.f * uniform24(A.seed, (uint32_t)i, 1u) - 1.f);
-        const float jz = A.jitter * (2.f * uniform24(A.seed, (uint32_t)i, 2u) - 1.f);
-        x = (ix + 0.5f + jx) * sx;
-        y = (iy + 0.5f + jy) * sy;
-        z = (iz + 0.5f + jz) * sz;
+        const float jx = __fmul_rn(A.jitter, 2.f * uniform24(A.seed, (uint32_t)i, 0u) - 1.f);
+        const float jy = __fmul_rn(A.jitter, 2.f * uniform24(A.seed, (uint32_t)i, 1u) - 1.f);
+        const float jz = __fmul_rn(A.jitter, 2.f * uniform24(A.seed, (uint32_t)i, 2u) - 1.f);
+        x = __fmul_rn(__fadd_rn((float)ix + 0.5f, jx), sx);
+        y = __fmul_rn(__fadd_rn((float)iy + 0.5f, jy), sy);
+        z = __fmul_rn(__fadd_rn((float)iz + 0.5f, jz), sz);
         th = theta_ref(P, z);
         for (int b = 0; b < A.nbub; ++b) {
             const float ddx = x - A.bx[b], ddy = y - A.by[b], ddz = z - A.bz[b];
@@ -54,10 +57,18 @@ __global__ void k_init(const __grid_constant__ Phys P, const __grid_constant__ I
         if (A.noise > 0.f) th += A.noise * normal01(A.seed, (uint32_t)i, 3u);
         qv = qv_ref(P, z);
     }
-    pos[i] = make_float4(x, y, z, rho_ref(P, z));
+    // The initial density is rho_ref(z).  The reference lattice takes the
+    // reference's float evaluation (asph_h100.cu:224); the config lattice
+    // takes the sounding table's value rounded once, so that the first
+    // density pass, whose p' = c_s^2 (rho - rho_ref) is a small residual
+    // there (the Shepard sum reproduces rho_ref in the interior), starts
+    // from the correctly rounded profile.
+    const float rho0 = A.mode == ASPH_INIT_REFERENCE ? rho_ref(P, z) : __fadd_rn(snd_eval(P.snd_rho, P.snd_n, z).hi,
+                                                                                 snd_eval(P.snd_rho, P.snd_n, z).lo);
+    pos[i] = make_float4(x, y, z, rho0);
     vel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     thq[i] = make_float4(th, qv, 0.f, 0.f);
-    rp[i] = make_float2(rho_ref(P, z), 0.f);
+    rp[i] = make_float2(rho0, 0.f);
     acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     dthdt[i] = 0.f;
 }
@@ -239,17 +250,23 @@ __global__ void k_clamp_done(DevCtl* ctl) { ctl->clamp_pending = 0; }
 
 // ---------------------------------------------------------------------------
 // FP64 conservation audit (asph_h100.cu:650-668), deterministic two-stage.
+// Every per-particle term is formed in double from the float32 state,
+// including the Exner function of the reference sounding, so that the six
+// totals are FP64 sums of FP64 terms.
 // ---------------------------------------------------------------------------
-__global__ void k_audit_partial(const __grid_constant__ Phys P, const float4* __restrict__ pos,
-                                const float4* __restrict__ vel, const float4* __restrict__ thq,
-                                double* __restrict__ partial) {
+__global__ void k_audit_partial(const __grid_constant__ Phys P, const __grid_constant__ AuditConst A,
+                                const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                const float4* __restrict__ thq, double* __restrict__ partial) {
+    constexpr double G_D = 9.80665, RD_D = 287.05, CP_D = 1004.0, P0_D = 100000.0;
     double a[5] = {0, 0, 0, 0, 0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.N; i += gridDim.x * blockDim.x) {
         const float4 p = pos[i], v = vel[i], t = thq[i];
-        const float Pi = powf(fmaxf(pres_ref(P, p.z), 1.f) / P0, R_D / CP);
+        const double ex = 1.0 - A.a_exner * (1.0 - exp(-A.n2 * (double)p.z / G_D));   // asph_h100.cu:139-142
+        const double pr = P0_D * pow(ex, CP_D / RD_D);                                 // asph_h100.cu:143-145
+        const double Pi = pow(fmax(pr, 1.0) / P0_D, RD_D / CP_D);
         a[0] += 0.5 * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
-        a[1] += (double)GRAV * p.z;
-        a[2] += (double)CP * t.x * Pi;
+        a[1] += G_D * p.z;
+        a[2] += CP_D * t.x * Pi;
         a[3] += (double)t.y + (double)t.z;
         a[4] += (double)v.z;
     }
@@ -263,14 +280,14 @@ __global__ void k_audit_partial(const __grid_constant__ Phys P, const float4* __
     }
     if (threadIdx.x < 5) partial[blockIdx.x * 5 + threadIdx.x] = s[threadIdx.x][0];
 }
-__global__ void k_audit_final(const __grid_constant__ Phys P, const double* __restrict__ partial, int nblk,
+__global__ void k_audit_final(const __grid_constant__ AuditConst A, const double* __restrict__ partial, int nblk,
                               double* __restrict__ out) {
     if (threadIdx.x < 5) {
         double acc = 0.0;
         for (int b = 0; b < nblk; ++b) acc += partial[b * 5 + threadIdx.x];
-        out[threadIdx.x] = acc * (double)P.pmass;
+        out[threadIdx.x] = acc * A.pmass;
     }
-    if (threadIdx.x == 5) out[5] = (double)P.pmass * (double)P.N;
+    if (threadIdx.x == 5) out[5] = A.pmass * (double)A.N;
 }
 
 // Surface-layer flags of the current order (exported surface list).
@@ -374,9 +391,10 @@ void launch_clamp(const Phys& P, const Bufs& B, cudaStream_t s) {
     k_clamp_done<<<1, 1, 0, s>>>(B.ctl);
 }
 
-void launch_audit(const Phys& P, const Bufs& B, double* partial, int nblk, double* out, cudaStream_t s) {
-    k_audit_partial<<<nblk, TPB, 0, s>>>(P, B.pos[B.pc], B.vel[B.vc], B.thq[B.qc], partial);
-    k_audit_final<<<1, 32, 0, s>>>(P, partial, nblk, out);
+void launch_audit(const Phys& P, const AuditConst& A, const Bufs& B, double* partial, int nblk, double* out,
+                  cudaStream_t s) {
+    k_audit_partial<<<nblk, TPB, 0, s>>>(P, A, B.pos[B.pc], B.vel[B.vc], B.thq[B.qc], partial);
+    k_audit_final<<<1, 32, 0, s>>>(A, partial, nblk, out);
 }
 
 void launch_surf_flags(const Phys& P, const Bufs& B, uint8_t* flags, cudaStream_t s) {

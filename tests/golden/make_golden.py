@@ -6,17 +6,23 @@ fixtures are produced by running the reference's own code:
   python tests/golden/make_golden.py helpers
       Compiles tests/golden/ref_helpers_host.cu, which #includes the
       reference file itself, for the host, and tabulates its host-callable
-      helpers (asph_h100.cu:136-171).  Needs the reference checkout
-      (ASPH_REFERENCE_SRC, default /root/reference/asph_h100.cu) and nvcc.
+      helpers (asph_h100.cu:136-171).  Needs the reference checkout (the
+      path oracle/build_oracle.py resolves, ASPH_REFERENCE_SRC) and nvcc.
       Writes tests/golden/ref_helpers.npz.
 
-  python tests/golden/make_golden.py gpu [outdir]
+  python tests/golden/make_golden.py gpu <outdir>
       On a GB300: runs the reference's kernels (oracle/_ref/asph_ref.cubin,
       built from the reference checkout by oracle/build_oracle.py) through
       oracle/refgpu on seeded synthetic states, one full reference step with
       every stage saved, plus the reference's own initial state.  Writes
-      ref_stages_<case>.npz and ref_init.npz into outdir (default
-      gpurun_out/golden); they are then committed under tests/golden/.
+      ref_stages_<case>.npz and ref_init.npz into outdir; they are then
+      committed under tests/golden/.
+
+  python tests/golden/make_golden.py dump <outdir>
+      On a GB300: runs this library's command-line driver on the small
+      reference-geometry case of tests/test_cli.py (DUMP_FIXTURE_ARGS) and
+      copies its last dump to <outdir>/ours_cli_dump.bin, the fixture that
+      the reference's own reader, tools/make_viz.py load(), is run on.
 
 All inputs are seeded synthetic states in the reference geometry
 (1000 m x 1000 m x 100 m cells, one particle per cell on average).
@@ -39,7 +45,10 @@ DX, DY, DZ = 1000.0, 1000.0, 100.0
 
 
 def make_helpers() -> None:
-    ref = os.environ.get("ASPH_REFERENCE_SRC", "/root/reference/asph_h100.cu")
+    from oracle import build_oracle
+    ref = build_oracle.REFERENCE_SRC
+    if not os.path.exists(ref):
+        raise SystemExit("reference checkout not found (set ASPH_REFERENCE_SRC)")
     with tempfile.TemporaryDirectory() as td:
         exe = os.path.join(td, "refhelpers")
         out = os.path.join(td, "h.bin")
@@ -179,11 +188,32 @@ def make_gpu(outdir: str) -> None:
         print("wrote init", N)
 
 
+# The command-line run whose last dump is the make_viz fixture: the
+# reference physics on a 16^3 grid, 0.02 h, dumps every 30 s, strides 4.
+DUMP_FIXTURE_ARGS = ["--nx", "16", "--ny", "16", "--nz", "16", "--dump-every", "30", "--sim-hours", "0.02",
+                     "--dump-stride", "4", "4", "--report", "50"]
+
+
+def make_dump(outdir: str) -> None:
+    import shutil
+    from sph_cuda_gb300 import _build
+    cli = _build.build_cli()
+    os.makedirs(outdir, exist_ok=True)
+    with tempfile.TemporaryDirectory() as td:
+        subprocess.check_call([cli, *DUMP_FIXTURE_ARGS, "--outdir", td], stdout=subprocess.DEVNULL)
+        last = sorted(f for f in os.listdir(td) if f.startswith("asph_t"))[-1]
+        shutil.copy(os.path.join(td, last), os.path.join(outdir, "ours_cli_dump.bin"))
+    print("wrote", os.path.join(outdir, "ours_cli_dump.bin"), "from", last)
+
+
 if __name__ == "__main__":
+    usage = "usage: make_golden.py helpers | gpu <outdir> | dump <outdir>"
     cmd = sys.argv[1] if len(sys.argv) > 1 else "helpers"
     if cmd == "helpers":
         make_helpers()
-    elif cmd == "gpu":
-        make_gpu(sys.argv[2] if len(sys.argv) > 2 else os.path.join(ROOT, "gpurun_out", "golden"))
+    elif cmd in ("gpu", "dump"):
+        if len(sys.argv) < 3:
+            raise SystemExit(usage)
+        (make_gpu if cmd == "gpu" else make_dump)(sys.argv[2])
     else:
-        raise SystemExit("usage: make_golden.py helpers | gpu [outdir]")
+        raise SystemExit(usage)

@@ -77,3 +77,30 @@ def test_bad_lattice_rejected():
     p.lat_nx = 31
     with pytest.raises(AsphError):
         check_params(p)
+
+
+def test_oracle_params_struct_is_the_library_layout():
+    from oracle import params as op
+    assert ctypes.sizeof(op.AsphParams) == ctypes.sizeof(abi.AsphParams)
+    ours = [(n, getattr(abi.AsphParams, n).offset, getattr(abi.AsphParams, n).size) for n, _ in abi.AsphParams._fields_]
+    theirs = [(n, getattr(op.AsphParams, n).offset, getattr(op.AsphParams, n).size) for n, _ in op.AsphParams._fields_]
+    assert ours == theirs
+
+
+@pytest.mark.parametrize("name,grid", [("reference", (0, 0, 0)), ("reference", (128, 128, 128)),
+                                       ("small65k", (0, 0, 0)), ("bubble2m", (0, 0, 0)), ("large16m", (0, 0, 0)),
+                                       ("adjoint262k", (0, 0, 0)), ("bubble2m", (66, 66, 0))])
+def test_oracle_presets_equal_the_library_presets(name, grid):
+    """The CPU benchmark legs build their parameters from the oracle's own
+    preset table; it must give the library's parameters bit for bit."""
+    from oracle import params as op
+    a = preset(name, *grid)
+    b = op.preset(name, *grid)
+    assert bytes(a) == bytes(b), [k for k in a.as_dict() if a.as_dict()[k] != b.as_dict()[k]]
+
+
+def test_oracle_workloads_equal_the_bench_workloads():
+    import bench
+    from oracle import params as op
+    for w in ("bubble2m", "bubble524k", "reference128", "large16m"):
+        assert bytes(bench.workload_params(w)) == bytes(op.workload(w)), w

@@ -1,8 +1,9 @@
 """Multi-process host logic of bench.py on CPU (gloo, world size 2).
 
-The path does not shard: N GPUs run N independent replicas, and the job
-rate is all units over the slowest rank's time.  The reference arm runs on
-rank 0 only; the other ranks exit 0 without output.
+The plain step would shard by slabs of cells, but the benchmark runs one
+GPU per process: N GPUs run N independent replicas, and the job rate is
+all units over the slowest rank's time.  The reference arm runs on rank 0
+only; the other ranks exit 0 without output.
 """
 import io
 import os
@@ -75,8 +76,26 @@ def test_workload_presets_match_their_descriptions():
     q = bench.workload_params("bubble524k")
     assert q.n_particles == 524288 and (q.nx, q.ny, q.nz) == (66, 66, 200)
     assert q.dx == pytest.approx(p.dx) and q.dz == pytest.approx(p.dz)
-    s = bench.cpu_sample_params()
-    assert s.n_particles == 131072 and s.dx == pytest.approx(p.dx)
+
+
+def test_reference_arm_loads_no_product_code():
+    """The reference arm times the oracle port on the full configuration
+    with the oracle's own parameters: it neither imports the product
+    package nor maps the CUDA library."""
+    import json
+    import subprocess
+    code = ("import sys, json; sys.path.insert(0, %r); import bench; "
+            "a = bench.parse_args(['--impl', 'reference', '--workload', 'bubble524k', '--steps', '1', '--warmup', '1']); "
+            "bench.run_reference(a); maps = open('/proc/self/maps').read(); "
+            "print(json.dumps({'pkg': any(m.startswith('sph_cuda_gb300') for m in sys.modules), "
+            "'so': 'libasph' in maps, 'oracle': 'liboracle' in maps}))" % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = [json.loads(ln) for ln in r.stdout.splitlines() if ln.startswith("{")]
+    line, chk = lines[0], lines[-1]
+    assert line["impl"] == "reference" and line["config"]["particles"] == 524288
+    assert line["cpu_baseline"]["kind"] == "port" and line["value"] > 0
+    assert chk == {"pkg": False, "so": False, "oracle": True}
 
 
 def test_other_workloads_and_options():

@@ -89,3 +89,24 @@ def test_cli_dumps_match_library(cli, tmp_path, validate):
         d = dumpfmt.read(str(out / fn))
         assert (d["nx"], d["cx"], d["cz"], d["sx"], d["sz"]) == (16, 4, 4, 4, 4)
     sim.close()
+
+
+@pytest.mark.gpu
+def test_cli_dump_reproduces_the_make_viz_fixture(cli, tmp_path):
+    """The committed fixture tests/golden/ours_cli_dump.bin (read by the
+    reference's own tools/make_viz.py load() in test_dump_format.py) is the
+    last dump of this run; the run still writes it."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_golden import DUMP_FIXTURE_ARGS
+    fx = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ours_cli_dump.bin")
+    if not os.path.exists(fx):
+        pytest.skip("fixture not generated (make_golden.py dump)")
+    out = tmp_path / "d"
+    r = _run(cli, *DUMP_FIXTURE_ARGS, "--outdir", out)
+    assert r.returncode == 0, r.stderr
+    last = sorted(os.listdir(out))[-1]
+    a, b = dumpfmt.read(str(out / last)), dumpfmt.read(fx)
+    for k in ("nx", "ny", "nz", "cx", "cy", "cz", "sx", "sy", "sz", "nfields", "t_sim", "dt", "lx", "ly", "lz"):
+        assert a[k] == b[k], k
+    assert np.allclose(a["data"], b["data"], rtol=1e-6, atol=0)

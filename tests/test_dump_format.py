@@ -28,3 +28,45 @@ def test_make_viz_struct_layout():
     assert h[0] == 0x41535048 and h[1] == 3
     vals = np.frombuffer(raw[68:], np.float32)
     assert vals.size == h[5] * h[6] * h[7] * h[11]
+
+
+def _make_viz():
+    """tools/make_viz.py of the reference checkout, imported by path (its
+    main() only runs as a script)."""
+    import importlib.util
+    import pytest
+    from oracle import build_oracle
+    path = os.path.join(os.path.dirname(build_oracle.REFERENCE_SRC), "tools", "make_viz.py")
+    if not os.path.exists(path):
+        pytest.skip("reference checkout not present (ASPH_REFERENCE_SRC)")
+    spec = importlib.util.spec_from_file_location("make_viz", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_make_viz_loads_a_dump_this_library_wrote():
+    """The consumer contract run for real: the reference's own reader,
+    make_viz.load() (make_viz.py:16-37), parses a dump written on a GB300 by
+    this library's command-line driver (fixture from make_golden.py dump),
+    and every value equals our reader's."""
+    import pytest
+    fx = os.path.join(GOLDEN, "ours_cli_dump.bin")
+    if not os.path.exists(fx):
+        pytest.skip("fixture not generated (make_golden.py dump)")
+    mv = _make_viz()
+    v = mv.load(fx)
+    d = dumpfmt.read(fx)
+    assert (v["nx"], v["ny"], v["nz"], v["cx"], v["cy"], v["cz"]) == (d["nx"], d["ny"], d["nz"], d["cx"], d["cy"],
+                                                                      d["cz"])
+    assert v["t"] == d["t_sim"] and (v["lx"], v["ly"], v["lz"]) == (d["lx"], d["ly"], d["lz"])
+    for c, name in enumerate(("theta", "qv", "ql", "u", "v", "w")):
+        assert np.array_equal(np.asarray(v["fields"][name], np.float32), d["data"][..., c]), name
+    assert np.all(d["data"][..., 0][d["data"][..., 0] != 0] > 250.0)   # theta of non-empty cells
+
+
+def test_make_viz_loads_the_reference_dump_fixture():
+    mv = _make_viz()
+    src = os.path.join(GOLDEN, "ref_dump_t300.bin")
+    v, d = mv.load(src), dumpfmt.read(src)
+    assert np.array_equal(np.asarray(v["fields"]["w"], np.float32), d["data"][..., 5])
