@@ -416,7 +416,9 @@ def run_ensemble(args):
     ens.sync()
     clk = clocks.stop()
     ms_ens = e0.elapsed_time(e1)
-    # the same members one after another, each through its own captured plain step
+    # the same members run sequentially through the plain step: member k
+    # runs its K graph-launched steps to completion before member k + 1
+    # starts (same tuned options, each member continuing from its state)
     views = [ens.member(k) for k in range(len(members))]
     for v in views:
         v.step(1)
@@ -424,9 +426,7 @@ def run_ensemble(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for v in views:
-        v.step_async(args.steps)
-    for v in views:
-        v.sync()
+        v.step(args.steps)   # returns when the member's steps are done
     ms_seq = (time.perf_counter() - t0) * 1e3
     line = {
         "metric": "aggregate particle-steps/s (64-member ensemble)", "value": total * args.steps / (ms_ens / 1e3),
@@ -438,12 +438,15 @@ def run_ensemble(args):
                    "particles_min": min(int(p.n_particles) for p in members),
                    "particles_max": max(int(p.n_particles) for p in members)},
         "sequential": {"value": total * args.steps / (ms_seq / 1e3), "ms_per_step": ms_seq / args.steps,
-                       "how": "each member's own graph-launched plain step, members one after another"},
+                       "how": "each member's own graph-launched plain step; member k runs its K steps to "
+                              "completion before member k+1 starts"},
         "speedup_vs_sequential": ms_seq / ms_ens,
         "tuning": {"seconds": t_tune, "chosen_shape_counts": {str(s): sum(1 for c in chosen if c[0] == s)
                                                                for s in sorted(set(c[0] for c in chosen))},
                    "chosen_sort_counts": {str(s): sum(1 for c in chosen if c[1] == s)
-                                          for s in sorted(set(c[1] for c in chosen))}},
+                                          for s in sorted(set(c[1] for c in chosen))},
+                   "chosen_targets_per_thread_counts": {str(s): sum(1 for c in chosen if c[2] == s)
+                                                        for s in sorted(set(c[2] for c in chosen))}},
         "gpu_launches": args.steps * member_kernels,
         "clocks": clk,
     }

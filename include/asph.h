@@ -229,10 +229,15 @@ int asph_step_profiled(asph_ctx* ctx, int nsteps, float* phase_ms);
  * the shape in use, -1 for the global path.  A shape whose staged region
  * does not suit the grid or the particle density is ASPH_ERR_ARG.
  * ASPH_OPT_SORT_EVERY: sort cadence, 0 = displacement-gated (the
- * reference), k > 0 = every k steps (the AsphParams field sort_every). */
+ * reference), k > 0 = every k steps (the AsphParams field sort_every).
+ * ASPH_OPT_TARGETS_PER_THREAD: targets each thread of the momentum pass
+ * takes, 1, 2 (default) or 4, so that a warp covers 32, 64 or 128
+ * consecutive targets (about 32 k / ppc cells, ppc = particles per cell);
+ * 0 restores the default.  Results do not depend on it. */
 #define ASPH_OPT_PAIR_PATH  1
 #define ASPH_OPT_PAIR_SHAPE 2
 #define ASPH_OPT_SORT_EVERY 3
+#define ASPH_OPT_TARGETS_PER_THREAD 4
 int asph_set_option(asph_ctx* ctx, int option, int value);
 int asph_get_option(asph_ctx* ctx, int option, int* value);
 
@@ -316,10 +321,12 @@ int asph_checkpoint_read(asph_ctx* ctx, const char* path);
  * asph_ens_member() lends a member's context for state, audit and dump calls
  * (ordered after the queued ensemble steps); the ensemble keeps ownership.
  * asph_ens_tune() times every brick shape that suits each member (and the
- * per-target path) crossed with the sort cadences in sort_choices (none:
- * keep each member's own), trial_steps steps each from a snapshot, keeps
- * the fastest per member and restores the member's state; chosen (may be
- * NULL) receives per member {shape (-1: per-target path), sort cadence}. */
+ * per-target path), crossed with the momentum pass's targets per thread
+ * (1, 2, 4: the cells one warp covers) and with the sort cadences in
+ * sort_choices (none: keep each member's own), trial_steps steps each from
+ * a snapshot, keeps the fastest per member and restores the member's
+ * state; chosen (may be NULL, else 3 ints per member) receives {shape (-1:
+ * per-target path), sort cadence, targets per thread}. */
 typedef struct asph_ens asph_ens;
 int asph_ens_create(const AsphParams* members, int n_members, void* stream, asph_ens** out);
 int asph_ens_destroy(asph_ens* ens);
@@ -365,18 +372,21 @@ int asph_set_viscosity(asph_ctx* ctx, float alpha, float beta);
  * cudaMalloc/cudaFree (a latency-critical loop where cudaFree would
  * synchronise the device, a host callback or foreign-language runtime that
  * must not block in the allocator, an application whose memory pool owns all
- * device memory): sorts n 32-bit keys (device pointer `keys`) over bits
- * [0, key_bits) stably, writing the sorted keys and the permutation
- * (sorted position -> input index) to caller-owned device buffers.  Same
- * kernels and same result as the sort of asph_sort_build.  Scratch lives in
- * a static device array sized for ASPH_NOALLOC_MAX_KEYS keys (about 5 MB,
+ * device memory): sorts n 32-bit keys (device pointer `keys`) stably,
+ * writing the sorted keys and the permutation (sorted position -> input
+ * index) to caller-owned device buffers.  Same kernels and same result as
+ * the sort of asph_sort_build.  The sort runs over whole 8-bit digits, bits
+ * [0, 8*ceil(key_bits/8)): keys must be below 2^key_bits (Morton keys of a
+ * grid are) for that to be the sort over bits [0, key_bits).  Scratch lives
+ * in a static device array sized for ASPH_NOALLOC_MAX_KEYS keys (about 5 MB,
  * held by every GPU that loads the library until exit); larger n returns
  * ASPH_ERR_ARG.  All calls share that array: calls that overlap on the GPU
  * race and must be serialised by the caller.  The outputs must not alias
- * `keys` or each other.  The first call on a device
- * looks up the array's address (make it before any stream capture).  The
- * call synchronises `stream` and returns ASPH_ERR_TIMEOUT if a bounded
- * device wait gave up. */
+ * `keys` or each other.  The first call in each CUDA context looks up the
+ * array's address in that context.  Every call waits for `stream` and
+ * reads the device error word back, so it must never be made while any
+ * stream on the device is being captured into a graph.  Returns
+ * ASPH_ERR_TIMEOUT if a bounded device wait gave up. */
 #define ASPH_NOALLOC_MAX_KEYS 524288
 int asph_sort_keys_noalloc(const uint32_t* keys, uint32_t* keys_sorted, uint32_t* perm, int n, int key_bits,
                            void* stream);

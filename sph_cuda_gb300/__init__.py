@@ -233,6 +233,15 @@ class Asph:
     def set_sort_every(self, k: int) -> None:
         _check(self.lib.asph_set_option(self._ctx, abi.OPT_SORT_EVERY, int(k)))
 
+    def targets_per_thread(self) -> int:
+        v = C.c_int()
+        _check(self.lib.asph_get_option(self._ctx, abi.OPT_TARGETS_PER_THREAD, C.byref(v)))
+        return v.value
+
+    def set_targets_per_thread(self, k: int) -> None:
+        """Momentum-pass targets per thread: 1, 2 or 4 (a warp covers 32 k targets)."""
+        _check(self.lib.asph_set_option(self._ctx, abi.OPT_TARGETS_PER_THREAD, int(k)))
+
     # ---- source-term hook ---------------------------------------------------------
     def enable_source(self, on: bool = True) -> None:
         """Per-particle additive tendencies of theta, qv, qc applied in every
@@ -399,12 +408,13 @@ class Ensemble:
         return m
 
     def tune(self, trial_steps: int = 5, sort_choices=()) -> list:
-        """Per member (shape, sort cadence) picked by timing; the state is kept."""
+        """Per member (brick shape, sort cadence, momentum targets per
+        thread) picked by timing; the state is kept."""
         n = len(self.params)
-        chosen = (C.c_int * (2 * n))()
+        chosen = (C.c_int * (3 * n))()
         sc = (C.c_int * max(1, len(sort_choices)))(*sort_choices)
         _check(self.lib.asph_ens_tune(self._h, int(trial_steps), sc, len(sort_choices), chosen))
-        return [(chosen[2 * k], chosen[2 * k + 1]) for k in range(n)]
+        return [(chosen[3 * k], chosen[3 * k + 1], chosen[3 * k + 2]) for k in range(n)]
 
 
 def ensemble_members(count: int = 64, seed: int = 7, lo: int = 16384, hi: int = 524288,

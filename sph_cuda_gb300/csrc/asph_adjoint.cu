@@ -490,7 +490,7 @@ __global__ void k_adj_dens_a(const Phys P, StepTape T, AdjBufs A) {
     for (int q = 0; q < cnt; ++q) {
         const int j = T.lst[(size_t)q * P.N + i];
         const float4 xj = T.pos1[j];
-        const float r2t = r2_cells(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z);   // the density pass's own r^2
+        const float r2t = r2_pair(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z);   // the density pass's own r^2
         if (r2t >= 4.f || r2t < 1e-12f) continue;
         const float qq = r2t * rsqrtf(r2t), t = 2.f - qq;
         const float W = qq < 1.f ? SIGMA_W * __fmaf_rn(qq * qq, __fmaf_rn(0.75f, qq, -1.5f), 1.f)
@@ -532,7 +532,7 @@ __global__ __launch_bounds__(ATPB) void k_adj_dens_b(const Phys P, StepTape T, A
         const int j = T.lst[(size_t)q * P.N + i];
         const float4 xj = T.pos1[j];
         const float2 lSj = A.lS[j];
-        const float r2t = r2_cells(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z);   // the density pass's own r^2
+        const float r2t = r2_pair(P, xi.x, xi.y, xi.z, xj.x, xj.y, xj.z);   // the density pass's own r^2
         if (r2t >= 4.f || r2t < 1e-12f) continue;
         const float rx = xi.x - xj.x, ry = xi.y - xj.y, rz = xi.z - xj.z;
         const float rs = rsqrtf(r2t), qq = r2t * rs, t = 2.f - qq;

@@ -374,6 +374,7 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
     B.perm = B.vbuf[(B.npasses - 1) & 1];
     B.pc = B.vc = B.qc = B.rc = 0;
     B.shape = -1;
+    B.m_tpt = 0;
     cudaStream_t s = c->stream;
     e = cudaMemsetAsync(B.status, 0, (size_t)B.npasses * B.ntiles * 256 * 8, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.inc_status, 0, (size_t)B.npasses * B.inc_tiles * 256 * 8, s);
@@ -436,13 +437,18 @@ extern "C" int asph_set_option(asph_ctx* c, int option, int value) {
         if (value < 0) return fail(ASPH_ERR_ARG, "sort cadence must be >= 0");
         c->P.sort_every = value;
         c->prm.sort_every = value;
+    } else if (option == ASPH_OPT_TARGETS_PER_THREAD) {
+        if (value != 0 && value != 1 && value != 2 && value != 4)
+            return fail(ASPH_ERR_ARG, "momentum targets per thread must be 1, 2 or 4 (0: default)");
+        c->B.m_tpt = value;
     } else {
         return fail(ASPH_ERR_ARG, "unknown option %d", option);
     }
     for (auto& g : c->gexec)   // captured graphs hold the old kernels and parameters
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     ++c->graph_epoch;
-    if (option != ASPH_OPT_SORT_EVERY) c->spans_valid = false;   // spans are per brick shape
+    if (option == ASPH_OPT_PAIR_PATH || option == ASPH_OPT_PAIR_SHAPE)
+        c->spans_valid = false;   // spans are per brick shape
     return ASPH_OK;
 }
 
@@ -458,6 +464,10 @@ extern "C" int asph_get_option(asph_ctx* c, int option, int* value) {
     }
     if (option == ASPH_OPT_SORT_EVERY) {
         *value = c->P.sort_every;
+        return ASPH_OK;
+    }
+    if (option == ASPH_OPT_TARGETS_PER_THREAD) {
+        *value = c->B.m_tpt > 0 ? c->B.m_tpt : 2;
         return ASPH_OK;
     }
     return fail(ASPH_ERR_ARG, "unknown option %d", option);

@@ -34,20 +34,19 @@ __device__ __forceinline__ FF snd_eval(const float4* __restrict__ tab, int nnode
 }
 
 // Pair distances in cell units.  Every acceptance test (brick and global
-// paths, the momentum fallback, the adjoint) uses these two functions, so
-// all of them accept exactly the same pairs: each coordinate is scaled to
-// cell units with one rounded product, the differences are exact float
-// subtractions, and r^2 is formed with explicit fused multiply-adds.
-__device__ __forceinline__ float3 to_cells(const Phys& P, float x, float y, float z) {
-    return make_float3(__fmul_rn(x, P.inv_dx), __fmul_rn(y, P.inv_dy), __fmul_rn(z, P.inv_dz));
-}
-__device__ __forceinline__ float r2_scaled(float ax, float ay, float az, float bx, float by, float bz) {
-    const float dx = ax - bx, dy = ay - by, dz = az - bz;
+// paths, the deferred pass, the momentum fallback, the adjoint) and every
+// density weight uses this one function, so all of them accept exactly the
+// same pairs: the coordinate differences are taken in metres first and then
+// scaled to cell units with one rounded product each, as the reference does
+// (asph_h100.cu:315-320), and r^2 is formed with explicit fused
+// multiply-adds.  (Scaling each position to cell units before differencing
+// would cost the pair ulp(x / dx), ~1.5e-5 cells at 133 cells, i.e. ~1e-5 of
+// a neighbour's weight.)  The momentum pair sum forms the same r^2.
+__device__ __forceinline__ float r2_pair(const Phys& P, float xi, float yi, float zi, float xj, float yj, float zj) {
+    const float dx = __fmul_rn(__fsub_rn(xi, xj), P.inv_dx);
+    const float dy = __fmul_rn(__fsub_rn(yi, yj), P.inv_dy);
+    const float dz = __fmul_rn(__fsub_rn(zi, zj), P.inv_dz);
     return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-}
-__device__ __forceinline__ float r2_cells(const Phys& P, float xi, float yi, float zi, float xj, float yj, float zj) {
-    const float3 a = to_cells(P, xi, yi, zi), b = to_cells(P, xj, yj, zj);
-    return r2_scaled(a.x, a.y, a.z, b.x, b.y, b.z);
 }
 
 // Stop the run from inside a kernel: record the reason (first one wins)
@@ -254,9 +253,9 @@ struct MTarget {
 __device__ __forceinline__ void msum_add(const Phys& P, MSum& s, const MTarget& T, float4 pj, float4 vj) {
     // pj = (x, y, z, p'_j), vj = (u, v, w, rho_j); FMAs and approximate
     // reciprocals throughout (relative error ~1e-7 per pair)
-    const float rx = T.x - pj.x, ry = T.y - pj.y, rz = T.z - pj.z;
-    const float dxt = rx * P.inv_dx, dyt = ry * P.inv_dy, dzt = rz * P.inv_dz;
-    const float r2t = __fmaf_rn(dxt, dxt, __fmaf_rn(dyt, dyt, dzt * dzt));
+    const float rx = __fsub_rn(T.x, pj.x), ry = __fsub_rn(T.y, pj.y), rz = __fsub_rn(T.z, pj.z);
+    const float dxt = __fmul_rn(rx, P.inv_dx), dyt = __fmul_rn(ry, P.inv_dy), dzt = __fmul_rn(rz, P.inv_dz);
+    const float r2t = __fmaf_rn(dxt, dxt, __fmaf_rn(dyt, dyt, __fmul_rn(dzt, dzt)));   // = r2_pair
     const float rs = rsqrtf(r2t);
     const float q = r2t * rs;
     const float t2 = 2.0f - q;

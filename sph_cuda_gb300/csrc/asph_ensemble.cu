@@ -403,9 +403,11 @@ extern "C" int asph_ens_step(asph_ens* e, int nsteps) {
 }
 
 // Autotuner: per member, every brick shape that suits its grid plus the
-// per-target path, crossed with the allowed sort cadences, each timed over
-// trial_steps graph-launched steps (after one untimed step) from the same
-// snapshot; the member keeps the fastest and its state is put back.
+// per-target path (the cells each density block covers), crossed with the
+// momentum pass's targets per thread (1, 2, 4: the cells each warp covers)
+// and the allowed sort cadences, each timed over trial_steps graph-launched
+// steps (after one untimed step) from the same snapshot; the member keeps
+// the fastest and its state is put back.
 extern "C" int asph_ens_tune(asph_ens* e, int trial_steps, const int* sort_choices, int n_sort_choices,
                              int* chosen) {
     if (!e || trial_steps < 1 || n_sort_choices < 0 || (n_sort_choices > 0 && !sort_choices))
@@ -430,12 +432,15 @@ extern "C" int asph_ens_tune(asph_ens* e, int trial_steps, const int* sort_choic
         for (int s = 0; s < pair_shape_count(); ++s)
             if (pair_shape_fits(c->P, s)) shapes.push_back(s);
         float best = 1e30f;
-        int best_shape = -1, best_sort = c->P.sort_every;
+        int best_shape = -1, best_sort = c->P.sort_every, best_tpt = 2;
+        const int tpts[3] = {1, 2, 4};
         for (int sh : shapes) {
             for (int cad : cadences) {
+              for (int tpt : tpts) {
                 if ((st = asph_set_option(c, ASPH_OPT_PAIR_PATH, sh == -2 ? 1 : 0))) break;
                 if ((st = asph_set_option(c, ASPH_OPT_PAIR_SHAPE, sh == -2 ? -1 : sh))) break;
                 if ((st = asph_set_option(c, ASPH_OPT_SORT_EVERY, cad))) break;
+                if ((st = asph_set_option(c, ASPH_OPT_TARGETS_PER_THREAD, tpt))) break;
                 if ((st = asph_snapshot_restore(c, snap))) break;
                 if ((st = asph_step(c, 1))) break;   // capture + warm
                 cudaError_t err = cudaEventRecord(t0, c->stream);
@@ -445,19 +450,23 @@ extern "C" int asph_ens_tune(asph_ens* e, int trial_steps, const int* sort_choic
                 if ((st = sync_status(c))) break;
                 float ms = 0.f;
                 cudaEventElapsedTime(&ms, t0, t1);
-                if (ms < best) { best = ms; best_shape = sh; best_sort = cad; }
+                if (ms < best) { best = ms; best_shape = sh; best_sort = cad; best_tpt = tpt; }
+              }
+              if (st) break;
             }
             if (st) break;
         }
         if (!st) st = asph_set_option(c, ASPH_OPT_PAIR_PATH, best_shape == -2 ? 1 : 0);
         if (!st) st = asph_set_option(c, ASPH_OPT_PAIR_SHAPE, best_shape == -2 ? -1 : best_shape);
         if (!st) st = asph_set_option(c, ASPH_OPT_SORT_EVERY, best_sort);
+        if (!st) st = asph_set_option(c, ASPH_OPT_TARGETS_PER_THREAD, best_tpt);
         if (!st) st = asph_snapshot_restore(c, snap);
         if (!st) st = sync_status(c);
         asph_snapshot_destroy(snap);
         if (!st && chosen) {
-            chosen[2 * k] = best_shape == -2 ? -1 : best_shape;
-            chosen[2 * k + 1] = best_sort;
+            chosen[3 * k] = best_shape == -2 ? -1 : best_shape;
+            chosen[3 * k + 1] = best_sort;
+            chosen[3 * k + 2] = best_tpt;
         }
         if (st) fail(st, "tuning member %zu: %s", k, asph_last_error());
     }

@@ -83,6 +83,7 @@ struct Bufs {
     int pc, vc, qc, rc; // current index of pos/vel/thq/rain ping-pong pairs
     int force_global;   // 1: pair passes take the per-target global path, 2: density warp per target
     int shape;          // brick shape index of the density pass, -1: automatic
+    int m_tpt;          // targets per thread of the momentum pass (1, 2 or 4; 0: the default, 2)
     cudaStream_t aux;   // second stream: the full sort runs beside the incremental one (a graph branch)
     cudaEvent_t ev_fork, ev_join;
     float4* src;        // source-term hook: per-particle tendencies (theta, qv, qc), NULL when off

@@ -15,11 +15,20 @@
 // the counters it needs; calls that overlap on the GPU (two streams, or two
 // host threads) race on it and must be serialised by the caller.
 //
-// Set-up: the first call on a device looks up the array's device address
-// with cudaGetSymbolAddress (host code only sees a host-side stand-in for
-// the symbol) and caches it per device; make that first call before any
-// stream capture.
+// Set-up: host code only sees a host-side stand-in for the array, so the
+// first call in a CUDA context looks up the array's device address with
+// cudaGetSymbolAddress, with that context current, and caches it for that
+// context.  The cache is keyed by the context itself (from the driver's
+// cuCtxGetCurrent), so a context created later on the same device, by a
+// device reset or by a foreign runtime with its own context, gets its own
+// look-up.
+//
+// Every call waits for its stream and reads the device error word back, so
+// the function must never be called while any stream on the device is
+// being captured into a CUDA graph.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <mutex>
 #include "asph_internal.cuh"
 #include "../../include/asph.h"
 
@@ -45,8 +54,55 @@ constexpr size_t NA_BYTES = NA_STATUS_OFF + (size_t)MAX_PASSES * NA_MAX_TILES * 
 // The scratch: control block, ping-pong keys and values, look-back words.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
-constexpr int NA_MAX_DEVICES = 64;
-unsigned char* g_scratch_ptr[NA_MAX_DEVICES] = {};
+// Device addresses of the array, one per CUDA context that called.
+constexpr int NA_MAX_CONTEXTS = 64;
+struct NaEntry {
+    CUcontext ctx;
+    unsigned char* ptr;
+};
+NaEntry g_scratch[NA_MAX_CONTEXTS] = {};
+int g_scratch_n = 0;
+std::mutex g_scratch_mu;
+
+// The calling thread's current driver context, through the runtime's
+// driver entry point (the library links the runtime only); NULL when the
+// runtime has not made a context current yet.
+CUcontext current_context() {
+    typedef CUresult (*GetCurrent)(CUcontext*);
+    static GetCurrent fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (GetCurrent)f;
+    });
+    CUcontext c = nullptr;
+    if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+    return c;
+}
+
+// The array's device address in the calling thread's current context,
+// looked up on the first call in that context.
+unsigned char* scratch_address() {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    CUcontext ctx = current_context();
+    if (ctx)
+        for (int k = 0; k < g_scratch_n; ++k)
+            if (g_scratch[k].ctx == ctx) return g_scratch[k].ptr;
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return nullptr;
+    ctx = current_context();   // the look-up makes the device's context current if none was
+    if (ctx) {
+        int slot = -1;
+        for (int k = 0; k < g_scratch_n; ++k)
+            if (g_scratch[k].ctx == ctx) slot = k;
+        if (slot < 0) slot = g_scratch_n < NA_MAX_CONTEXTS ? g_scratch_n++ : NA_MAX_CONTEXTS - 1;
+        g_scratch[slot] = NaEntry{ctx, (unsigned char*)p};
+    }
+    return (unsigned char*)p;
+}
 
 __global__ void k_noalloc_prep(DevCtl* ctl) {
     for (int i = threadIdx.x; i < MAX_PASSES * 256; i += blockDim.x) (&ctl->hist[0][0])[i] = 0u;
@@ -72,16 +128,8 @@ extern "C" int asph_sort_keys_noalloc(const uint32_t* keys, uint32_t* keys_sorte
     if (key_bits < 1 || key_bits > 8 * MAX_PASSES) return na_fail(ASPH_ERR_ARG, "asph_sort_keys_noalloc: key_bits outside [1, 32]");
     if (n == 0) return ASPH_OK;
     if (!keys || !keys_sorted || !perm) return na_fail(ASPH_ERR_ARG, "asph_sort_keys_noalloc: NULL pointer");
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES)
-        return na_fail(ASPH_ERR_CUDA, "asph_sort_keys_noalloc: no current device");
-    if (!g_scratch_ptr[dev]) {   // once per device, with that device current
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) return na_fail(ASPH_ERR_CUDA, "asph_sort_keys_noalloc: cudaGetSymbolAddress failed");
-        g_scratch_ptr[dev] = (unsigned char*)p;
-    }
-    unsigned char* base = g_scratch_ptr[dev];
+    unsigned char* base = scratch_address();
+    if (!base) return na_fail(ASPH_ERR_CUDA, "asph_sort_keys_noalloc: cudaGetSymbolAddress failed");
     DevCtl* ctl = reinterpret_cast<DevCtl*>(base);
     uint32_t* sk = reinterpret_cast<uint32_t*>(base + NA_KEYS_OFF);
     uint32_t* sv = reinterpret_cast<uint32_t*>(base + NA_VALS_OFF);
@@ -105,10 +153,11 @@ extern "C" int asph_sort_keys_noalloc(const uint32_t* keys, uint32_t* keys_sorte
         vi = vo;
     }
     if (cudaGetLastError() != cudaSuccess) return na_fail(ASPH_ERR_CUDA, "asph_sort_keys_noalloc: launch failed");
-    if (cudaStreamSynchronize(s) != cudaSuccess) return na_fail(ASPH_ERR_CUDA, "asph_sort_keys_noalloc: kernel failed");
+    // read the error word on the caller's stream only (no device-wide wait)
     int err = 0;
-    if (cudaMemcpy(&err, &ctl->error, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    if (cudaMemcpyAsync(&err, &ctl->error, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
         return na_fail(ASPH_ERR_CUDA, "asph_sort_keys_noalloc: cannot read the error word");
+    if (cudaStreamSynchronize(s) != cudaSuccess) return na_fail(ASPH_ERR_CUDA, "asph_sort_keys_noalloc: kernel failed");
     if (err) return na_fail(ASPH_ERR_TIMEOUT, "asph_sort_keys_noalloc: a bounded look-back wait gave up");
     return ASPH_OK;
 }

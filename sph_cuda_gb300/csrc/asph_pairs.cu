@@ -47,7 +47,7 @@ constexpr int MAX_HALO = 3;      // widest staged halo (cells around a brick)
 constexpr int DENSITY_REGS = 48; // register cap of the brick kernel (its launch plan counts on it)
 constexpr int DLIST = 30;        // most queued accepted candidates per thread (D); a launch may use fewer
 constexpr int M_TPB = 256;
-constexpr int M_TPT = 2;         // targets per thread of the momentum pass
+constexpr int M_TPT = 2;         // default targets per thread of the momentum pass (1, 2 or 4 per launch)
 
 template <int BX, int BY, int BZ, int H>
 struct BrickGeom {
@@ -284,7 +284,7 @@ __device__ __forceinline__ DSum density_target_global(const Phys& P, const DArgs
     NbrOut L{A.nbr, 0, P.N, i};
     for_window_global(P, A.range, A.ctl, pi.x, pi.y, pi.z, [&](int j) {
         const float4 pj = A.pos[j];
-        const float r2 = r2_cells(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z);
+        const float r2 = r2_pair(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z);
         if (r2 < 4.0f) {
             dsum_add(s, r2, pj.w, rr);
             if (r2 >= 1e-12f) L.push(j);
@@ -307,7 +307,7 @@ __global__ __launch_bounds__(256) void k_density_global(const __grid_constant__ 
 
 // Pointers into the density pass's dynamic shared memory.
 struct DSmem {
-    float4* sp;               // staged particles: x, y, z in cell units, rho_old
+    float4* sp;               // staged particles: x, y, z, rho_old
     int* s_gidx;              // global index of a staged slot
     int* s_off;               // region cell -> first slot (R + 1)
     int* s_start;             // region cell -> first global index (R)
@@ -373,10 +373,7 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int k = kb + u * T;
-                if (k < total) {
-                    const float3 c = to_cells(P, q[u].x, q[u].y, q[u].z);   // compared in cell units
-                    sp[k] = make_float4(c.x, c.y, c.z, q[u].w);
-                }
+                if (k < total) sp[k] = q[u];
             }
         }
     }
@@ -388,14 +385,12 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
         const int i = base + lane;
         const bool active = i < te;
         float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
-        float3 ci = make_float3(0.f, 0.f, 0.f);   // pi in cell units
         FF rr{0.f, 0.f};
         DSum s{0.f, 0.f, 0.f};
         int lx = 0, ly = 0, zlo = 0, zhi = -1;
         bool fast = false;
         if (active) {
             pi = A.pos[i];
-            ci = to_cells(P, pi.x, pi.y, pi.z);
             rr = snd_eval(P.snd_rho, P.snd_n, pi.z);
             fast = staged && local_window<BX, BY, BZ, H>(P, ox, oy, oz, pi.x, pi.y, pi.z, lx, ly, zlo, zhi);
         }
@@ -418,7 +413,7 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
             if (q < n) {                                                              \
                 const int kq = s_list[q * T + threadIdx.x];                           \
                 const float4 pj = sp[kq];                                             \
-                const float r2 = r2_scaled(ci.x, ci.y, ci.z, pj.x, pj.y, pj.z);       \
+                const float r2 = r2_pair(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z);      \
                 dsum_add(s, r2, pj.w, rr);                                            \
                 if (r2 >= 1e-12f) L.push(s_gidx[kq]);                                 \
             }                                                                         \
@@ -458,7 +453,7 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
                 }
                 const bool valid = k < kend;
                 const float4 pj = sp[valid ? k : 0];
-                if (valid && r2_scaled(ci.x, ci.y, ci.z, pj.x, pj.y, pj.z) < 4.0f)
+                if (valid && r2_pair(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z) < 4.0f)
                     s_list[(n++) * T + threadIdx.x] = (unsigned short)k;
                 k += valid ? 1 : 0;
             }
@@ -571,7 +566,6 @@ __global__ __launch_bounds__(DEF_TPB) void k_density_deferred(const __grid_const
             if (lane == 0) stop_run(ctl, ASPH_ERR_DENSE);
             break;
         }
-        const float3 ci = to_cells(P, pi.x, pi.y, pi.z);
         const FF rr = snd_eval(P.snd_rho, P.snd_n, pi.z);
         DSum s{0.f, 0.f, 0.f};
         int nb = 0;
@@ -600,8 +594,7 @@ __global__ __launch_bounds__(DEF_TPB) void k_density_deferred(const __grid_const
             const int j = jr[h];
             if (g < total) {
                 const float4 pj = pr[h];
-                const float3 cj = to_cells(P, pj.x, pj.y, pj.z);
-                const float r2 = r2_scaled(ci.x, ci.y, ci.z, cj.x, cj.y, cj.z);
+                const float r2 = r2_pair(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z);
                 if (r2 < 4.0f) {
                     dsum_add(s, r2, pj.w, rr);
                     push = r2 >= 1e-12f;
@@ -669,7 +662,7 @@ __device__ __noinline__ MSum momentum_target_global(const Phys& P, const MArgs& 
     MSum s{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for_window_global(P, A.range, A.ctl, T.x, T.y, T.z, [&](int j) {
         const float4 pj = A.pos[j];
-        const float r2t = r2_cells(P, T.x, T.y, T.z, pj.x, pj.y, pj.z);
+        const float r2t = r2_pair(P, T.x, T.y, T.z, pj.x, pj.y, pj.z);
         if (r2t >= 4.0f || r2t < 1e-12f) return;   // also excludes j == i
         const float2 rj = A.rp[j];
         const float4 vj = A.vel[j];
@@ -678,6 +671,7 @@ __device__ __noinline__ MSum momentum_target_global(const Phys& P, const MArgs& 
     return s;
 }
 
+template <int TPT>
 __global__ __launch_bounds__(M_TPB, 4) void k_momentum(const __grid_constant__ Phys P, const __grid_constant__ MArgs A,
                                                     int mode) {
     __shared__ float s_max[3][M_TPB / 32];
@@ -691,11 +685,11 @@ __global__ __launch_bounds__(M_TPB, 4) void k_momentum(const __grid_constant__ P
         const int cid = (blockIdx.x - A.part_blocks) * blockDim.x + threadIdx.x;
         if (cid < P.ncell && !aborted) rain_cell(P, cid, dt, A.rain_in, A.rain_delta, A.rain_out, A.precip);
     } else {
-        // M_TPT targets per thread, the lanes of warp w on targets w * 32 * M_TPT + lane + 32 r:
+        // TPT targets per thread, the lanes of warp w on targets w * 32 * TPT + lane + 32 r:
         // a warp waits on the longest sum of its lanes' lists rather than on the longest list
-        // of each round
-        const int tbase = blockIdx.x * (M_TPB * M_TPT) + (threadIdx.x >> 5) * (32 * M_TPT) + (threadIdx.x & 31);
-        for (int r = 0; r < M_TPT; ++r) {
+        // of each round; a warp covers 32 TPT consecutive targets, about 32 TPT / ppc cells
+        const int tbase = blockIdx.x * (M_TPB * TPT) + (threadIdx.x >> 5) * (32 * TPT) + (threadIdx.x & 31);
+        for (int r = 0; r < TPT; ++r) {
             const int i = tbase + 32 * r;
             if (i < P.N) {
                 if (aborted) {
@@ -1002,9 +996,16 @@ void launch_momentum(const Phys& P, const Bufs& B, int mode, int use_lists, cuda
     A.rain_out = B.rain[1 - B.rc];
     A.precip = B.precip;
     A.ctl = B.ctl;
-    A.part_blocks = blocks_for(P.N, M_TPB * M_TPT);
+    const int tpt = B.m_tpt > 0 ? B.m_tpt : M_TPT;
+    A.part_blocks = blocks_for(P.N, M_TPB * tpt);
     const int rain_blocks = (mode & M_RAIN) ? blocks_for(P.ncell, M_TPB) : 0;
-    k_momentum<<<A.part_blocks + rain_blocks, M_TPB, 0, s>>>(P, A, mode);
+    const int grid = A.part_blocks + rain_blocks;
+    if (tpt == 1)
+        k_momentum<1><<<grid, M_TPB, 0, s>>>(P, A, mode);
+    else if (tpt == 4)
+        k_momentum<4><<<grid, M_TPB, 0, s>>>(P, A, mode);
+    else
+        k_momentum<2><<<grid, M_TPB, 0, s>>>(P, A, mode);
 }
 
 }  // namespace asph

@@ -156,14 +156,14 @@ def test_tuner_keeps_state_and_choices_reproduce_solo_runs():
     before = [ens.member(k).get_state() for k in range(2)]
     chosen = ens.tune(trial_steps=2, sort_choices=(1, 2))
     assert len(chosen) == 2
-    for k, (shape, cad) in enumerate(chosen):
-        assert shape in (-1, 0, 1, 2, 3) and cad in (1, 2)
+    for k, (shape, cad, tpt) in enumerate(chosen):
+        assert shape in (-1, 0, 1, 2, 3) and cad in (1, 2) and tpt in (1, 2, 4)
         m = ens.member(k)
         _same(before[k], m.get_state())
         assert m.control()["step"] == 2
-        assert m.sort_every() == cad
+        assert m.sort_every() == cad and m.targets_per_thread() == tpt
     ens.step(3)
-    for k, (shape, cad) in enumerate(chosen):
+    for k, (shape, cad, tpt) in enumerate(chosen):
         solo = Asph(ms[k])
         solo.init()
         solo.step(2)
@@ -172,6 +172,7 @@ def test_tuner_keeps_state_and_choices_reproduce_solo_runs():
         else:
             solo.set_pair_shape(shape)
         solo.set_sort_every(cad)
+        solo.set_targets_per_thread(tpt)
         solo.step(3)
         _same(ens.member(k).get_state(), solo.get_state())
         solo.close()
@@ -186,3 +187,20 @@ def test_pair_shape_option_validates():
         sim.set_pair_shape(7)
     sim.set_pair_shape(-1)
     sim.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tpt", [1, 4])
+def test_momentum_targets_per_thread_do_not_change_results(tpt):
+    """The momentum pass's targets per thread (the cells one warp covers)
+    is a launch shape only: states are bit-identical to the default's."""
+    p = small_config()
+    a, b = Asph(p), Asph(p)
+    a.init(); b.init()
+    b.set_targets_per_thread(tpt)
+    assert b.targets_per_thread() == tpt and a.targets_per_thread() == 2
+    a.step(4); b.step(4)
+    _same(a.get_state(), b.get_state())
+    with pytest.raises(sph.AsphError):
+        b.set_targets_per_thread(3)
+    a.close(); b.close()

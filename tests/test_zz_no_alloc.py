@@ -67,6 +67,21 @@ def test_noalloc_sort_matches_sort_build_twice():
         assert np.array_equal(got_sorted, ref_sorted)
 
 
+def test_noalloc_sort_at_the_size_limit():
+    """n = ASPH_NOALLOC_MAX_KEYS, where the scratch buffers are full: random
+    30-bit keys, twice in a row, against numpy's stable argsort."""
+    torch = pytest.importorskip("torch")
+    lib = abi.load_library()
+    rng = np.random.default_rng(23)
+    for _ in range(2):
+        keys = rng.integers(0, 1 << 30, abi.NOALLOC_MAX_KEYS, dtype=np.uint32)
+        keys[:1000] = keys[1000:2000]   # ties: stability matters
+        got_sorted, got_perm = _noalloc(lib, torch, keys, 30)
+        ref_perm = np.argsort(keys, kind="stable").astype(np.uint32)
+        assert np.array_equal(got_perm, ref_perm)
+        assert np.array_equal(got_sorted, keys[ref_perm])
+
+
 def test_noalloc_sort_rejects_oversize():
     lib = abi.load_library()
     n = abi.NOALLOC_MAX_KEYS + 1
