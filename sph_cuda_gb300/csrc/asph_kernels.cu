@@ -58,13 +58,23 @@ __global__ void k_init(const __grid_constant__ Phys P, const __grid_constant__ I
         qv = qv_ref(P, z);
     }
     // The initial density is rho_ref(z).  The reference lattice takes the
-    // reference's float evaluation (asph_h100.cu:224); the config lattice
-    // takes the sounding table's value rounded once, so that the first
-    // density pass, whose p' = c_s^2 (rho - rho_ref) is a small residual
-    // there (the Shepard sum reproduces rho_ref in the interior), starts
-    // from the correctly rounded profile.
-    const float rho0 = A.mode == ASPH_INIT_REFERENCE ? rho_ref(P, z) : __fadd_rn(snd_eval(P.snd_rho, P.snd_n, z).hi,
-                                                                                 snd_eval(P.snd_rho, P.snd_n, z).lo);
+    // reference's float evaluation (asph_h100.cu:224).  The config lattice
+    // evaluates the sounding in double (asph_h100.cu:136-146) and rounds
+    // once: there p' = c_s^2 (rho - rho_ref) of the first density pass is a
+    // small residual (the Shepard sum reproduces rho_ref in the interior),
+    // and one float ulp of a particle's starting density moves its p' by
+    // ~2e-4 Pa, so the start must be the correctly rounded profile.
+    float rho0;
+    if (A.mode == ASPH_INIT_REFERENCE) {
+        rho0 = rho_ref(P, z);
+    } else {
+        constexpr double G_D = 9.80665, RD_D = 287.05, CP_D = 1004.0, P0_D = 100000.0;
+        const double th0 = P.th0, n2 = P.n2, zd = z;
+        const double a = G_D * G_D / (CP_D * th0 * n2);
+        const double th = th0 * exp(n2 * zd / G_D);
+        const double ex = 1.0 - a * (1.0 - exp(-n2 * zd / G_D));
+        rho0 = (float)(P0_D * pow(ex, CP_D / RD_D) / (RD_D * th * ex));
+    }
     pos[i] = make_float4(x, y, z, rho0);
     vel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     thq[i] = make_float4(th, qv, 0.f, 0.f);
