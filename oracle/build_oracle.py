@@ -21,7 +21,13 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_SRC = os.environ.get("ASPH_REFERENCE_SRC", "/root/reference/asph_h100.cu")
+
+
+def reference_src() -> str:
+    """Path of the reference's asph_h100.cu, from ASPH_REFERENCE_SRC; empty
+    when it is unset (the recipes that need the checkout then skip)."""
+    return os.environ.get("ASPH_REFERENCE_SRC", "")
+
 LIBORACLE = os.path.join(BUILD, "liboracle.so")
 LIBADJHOST = os.path.join(BUILD, "libadjhost.so")
 CUBIN = os.path.join(REF_OUT, "asph_ref.cubin")
@@ -70,11 +76,12 @@ def build_adjoint_host(force: bool = False) -> str:
 
 def build_ref_cubin(force: bool = False) -> str:
     """Compile the reference's kernels into a cubin (needs the checkout)."""
-    if not os.path.exists(REFERENCE_SRC):
+    src = reference_src()
+    if not src or not os.path.exists(src):
         return CUBIN if os.path.exists(CUBIN) else ""
     os.makedirs(REF_OUT, exist_ok=True)
-    if force or _stale(CUBIN, [REFERENCE_SRC]):
-        _run([_nvcc(), "-cubin", "-O3", "-use_fast_math", "-std=c++17", *ARCH, "-o", CUBIN, REFERENCE_SRC])
+    if force or _stale(CUBIN, [src]):
+        _run([_nvcc(), "-cubin", "-O3", "-use_fast_math", "-std=c++17", *ARCH, "-o", CUBIN, src])
     return CUBIN
 
 
@@ -92,12 +99,13 @@ _GEOMETRY_LINES = {
 
 
 def build_ref_cubin_bubble2m(force: bool = False) -> str:
-    if not os.path.exists(REFERENCE_SRC):
+    src = reference_src()
+    if not src or not os.path.exists(src):
         return BUBBLE2M_CUBIN if os.path.exists(BUBBLE2M_CUBIN) else ""
     os.makedirs(REF_OUT, exist_ok=True)
-    if force or _stale(BUBBLE2M_CUBIN, [REFERENCE_SRC]):
+    if force or _stale(BUBBLE2M_CUBIN, [src]):
         import tempfile
-        text = open(REFERENCE_SRC).read()
+        text = open(src).read()
         for old, new in _GEOMETRY_LINES.items():
             if old not in text:
                 raise RuntimeError("reference constexpr line not found: " + old)

@@ -6,8 +6,8 @@ fixtures are produced by running the reference's own code:
   python tests/golden/make_golden.py helpers
       Compiles tests/golden/ref_helpers_host.cu, which #includes the
       reference file itself, for the host, and tabulates its host-callable
-      helpers (asph_h100.cu:136-171).  Needs the reference checkout (the
-      path oracle/build_oracle.py resolves, ASPH_REFERENCE_SRC) and nvcc.
+      helpers (asph_h100.cu:136-171).  Needs the reference checkout
+      (ASPH_REFERENCE_SRC = the path of its asph_h100.cu) and nvcc.
       Writes tests/golden/ref_helpers.npz.
 
   python tests/golden/make_golden.py gpu <outdir>
@@ -23,6 +23,12 @@ fixtures are produced by running the reference's own code:
       reference-geometry case of tests/test_cli.py (DUMP_FIXTURE_ARGS) and
       copies its last dump to <outdir>/ours_cli_dump.bin, the fixture that
       the reference's own reader, tools/make_viz.py load(), is run on.
+
+  python tests/golden/make_golden.py viz
+      Runs the reference's own reader, tools/make_viz.py load() (next to
+      ASPH_REFERENCE_SRC in the checkout), on tests/golden/ours_cli_dump.bin
+      and saves what it returns as tests/golden/make_viz_ours.npz, so that
+      machines without the checkout still compare our reader with it.
 
 All inputs are seeded synthetic states in the reference geometry
 (1000 m x 1000 m x 100 m cells, one particle per cell on average).
@@ -46,8 +52,8 @@ DX, DY, DZ = 1000.0, 1000.0, 100.0
 
 def make_helpers() -> None:
     from oracle import build_oracle
-    ref = build_oracle.REFERENCE_SRC
-    if not os.path.exists(ref):
+    ref = build_oracle.reference_src()
+    if not ref or not os.path.exists(ref):
         raise SystemExit("reference checkout not found (set ASPH_REFERENCE_SRC)")
     with tempfile.TemporaryDirectory() as td:
         exe = os.path.join(td, "refhelpers")
@@ -206,11 +212,44 @@ def make_dump(outdir: str) -> None:
     print("wrote", os.path.join(outdir, "ours_cli_dump.bin"), "from", last)
 
 
+def load_make_viz():
+    """tools/make_viz.py of the reference checkout (next to the file that
+    ASPH_REFERENCE_SRC names), imported by path: its main() only runs as a
+    script.  None when the checkout is not present."""
+    import importlib.util
+    from oracle import build_oracle
+    ref = build_oracle.reference_src()
+    path = os.path.join(os.path.dirname(ref), "tools", "make_viz.py") if ref else ""
+    if not path or not os.path.exists(path):
+        return None
+    spec = importlib.util.spec_from_file_location("make_viz", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+VIZ_FIELDS = ("theta", "qv", "ql", "u", "v", "w")
+
+
+def make_viz() -> None:
+    mv = load_make_viz()
+    if mv is None:
+        raise SystemExit("reference checkout not found (set ASPH_REFERENCE_SRC)")
+    v = mv.load(os.path.join(HERE, "ours_cli_dump.bin"))
+    head = np.array([v["nx"], v["ny"], v["nz"], v["cx"], v["cy"], v["cz"]], np.int64)
+    dims = np.array([v["t"], v["lx"], v["ly"], v["lz"]], np.float64)
+    fields = {k: np.asarray(v["fields"][k], np.float32) for k in VIZ_FIELDS}
+    np.savez_compressed(os.path.join(HERE, "make_viz_ours.npz"), head=head, dims=dims, **fields)
+    print("wrote", os.path.join(HERE, "make_viz_ours.npz"))
+
+
 if __name__ == "__main__":
-    usage = "usage: make_golden.py helpers | gpu <outdir> | dump <outdir>"
+    usage = "usage: make_golden.py helpers | viz | gpu <outdir> | dump <outdir>"
     cmd = sys.argv[1] if len(sys.argv) > 1 else "helpers"
     if cmd == "helpers":
         make_helpers()
+    elif cmd == "viz":
+        make_viz()
     elif cmd in ("gpu", "dump"):
         if len(sys.argv) < 3:
             raise SystemExit(usage)

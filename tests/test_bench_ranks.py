@@ -1,8 +1,9 @@
 """Multi-process host logic of bench.py on CPU (gloo, world size 2).
 
-The plain step would shard by slabs of cells, but the benchmark runs one
-GPU per process: N GPUs run N independent replicas, and the job rate is
-all units over the slowest rank's time.  The reference arm runs on rank 0
+The plain step shards by z-slabs of cells (sph_cuda_gb300.slabs, tested in
+test_slabs.py), but the benchmark's headline runs one full configuration
+per GPU: N GPUs run N independent replicas, and the job rate is all units
+over the slowest rank's time.  The reference arm runs on rank 0
 only; the other ranks exit 0 without output.
 """
 import io

@@ -1,6 +1,7 @@
 """Dump format (asph_h100.cu:743-747, 1106-1120; read by tools/make_viz.py)."""
 import os
 import struct
+import sys
 
 import numpy as np
 
@@ -31,18 +32,30 @@ def test_make_viz_struct_layout():
 
 
 def _make_viz():
-    """tools/make_viz.py of the reference checkout, imported by path (its
-    main() only runs as a script)."""
-    import importlib.util
+    """tools/make_viz.py of the reference checkout (ASPH_REFERENCE_SRC),
+    imported by path; skips where the checkout is not present."""
     import pytest
-    from oracle import build_oracle
-    path = os.path.join(os.path.dirname(build_oracle.REFERENCE_SRC), "tools", "make_viz.py")
-    if not os.path.exists(path):
-        pytest.skip("reference checkout not present (ASPH_REFERENCE_SRC)")
-    spec = importlib.util.spec_from_file_location("make_viz", path)
-    mod = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(mod)
-    return mod
+    sys.path.insert(0, GOLDEN)
+    from make_golden import load_make_viz
+    mv = load_make_viz()
+    if mv is None:
+        pytest.skip("reference checkout not present (ASPH_REFERENCE_SRC unset)")
+    return mv
+
+
+def test_our_reader_equals_make_viz_on_a_dump_this_library_wrote():
+    """What the reference's own reader, make_viz.load() (make_viz.py:16-37),
+    returned for the dump our command-line driver wrote on a GB300
+    (tests/golden/make_viz_ours.npz, made by make_golden.py viz) equals our
+    reader's parse of the same file, value for value; runs everywhere."""
+    fx = os.path.join(GOLDEN, "ours_cli_dump.bin")
+    v = np.load(os.path.join(GOLDEN, "make_viz_ours.npz"))
+    d = dumpfmt.read(fx)
+    assert list(v["head"]) == [d["nx"], d["ny"], d["nz"], d["cx"], d["cy"], d["cz"]]
+    assert v["dims"][0] == np.float32(d["t_sim"])
+    assert tuple(v["dims"][1:]) == (d["lx"], d["ly"], d["lz"])
+    for c, name in enumerate(("theta", "qv", "ql", "u", "v", "w")):
+        assert np.array_equal(v[name], d["data"][..., c]), name
 
 
 def test_make_viz_loads_a_dump_this_library_wrote():
