@@ -11,8 +11,11 @@ momentum/integrate/rain/CFL, one CUDA graph per step) timed with CUDA events
 on the simulation stream; one JSON line on rank 0.  Beside it: the per-kernel
 times over the same K states, the reference's own kernels on this GPU
 (`reference_gpu`) and the FP64 CPU port (`cpu_baseline`), both from the same
-initial state.  --impl reference times the CPU restatement of the reference
-(FP64, all host cores) on the full configuration.
+initial state, and the two other forms at their own configurations
+(`forms`: the 64-member ensemble against its members run one after another,
+the adjoint step against the plain step).  --impl reference times the CPU
+restatement of the reference (FP64, all host cores) on the full
+configuration.
 """
 from __future__ import annotations
 
@@ -342,10 +345,12 @@ def run_ours(args):
     nbytes = len(fields) * 4 * N
     sim.close()
 
-    cpu, ref_gpu = None, None
+    cpu, ref_gpu, forms = None, None, None
     if rank == 0 and ws == 1:
         if not args.no_reference_gpu:
             ref_gpu = reference_gpu(args, value)
+        if not args.no_forms and args.workload == "bubble2m":
+            forms = measure_forms()
         if not args.no_cpu:
             tc, nsteps, cores = oracle_timed(p, args.warmup, args.cpu_steps)
             cpu = {"value": N * nsteps / tc, "unit": UNIT, "cores": cores, "kind": "port",
@@ -374,6 +379,7 @@ def run_ours(args):
                          "step_bytes_per_particle": algo["step"] / N},
             "cpu_baseline": cpu,
             "reference_gpu": ref_gpu,
+            "forms": forms,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "steps": e2e_steps, "api": "asph_set_state + asph_step(1) + asph_get_state, pinned host SoA"},
             "gpu_launches": per_step * args.steps,
@@ -388,29 +394,36 @@ def run_ours(args):
 
 
 def run_ensemble(args):
+    import torch
+    torch.cuda.set_device(0)
+    line = measure_ensemble(args.steps, args.warmup, tune=not args.no_tune)
+    print(json.dumps(line))
+    return 0
+
+
+def measure_ensemble(steps: int, warmup: int, tune: bool = True) -> dict:
     """64 members of uneven size stepped together (one graph launch per
     ensemble step) against the same members stepped one after another
     through the plain step, with the same tuned options."""
     import torch
     import sph_cuda_gb300 as sph
 
-    torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
     members = sph.ensemble_members(64, seed=7)
     total = sum(int(p.n_particles) for p in members)
     ens = sph.Ensemble(members, stream=stream.cuda_stream)
     ens.init()
     t0 = time.perf_counter()
-    chosen = ens.tune(trial_steps=3, sort_choices=(0, 1, 2)) if not args.no_tune else []
+    chosen = ens.tune(trial_steps=3, sort_choices=(0, 1, 2)) if tune else []
     t_tune = time.perf_counter() - t0
-    ens.step(args.warmup)
+    ens.step(warmup)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(0)
     torch.cuda.synchronize()
     clocks.start()
     time.sleep(0.3)
     e0.record(stream)
-    ens.step_async(args.steps)
+    ens.step_async(steps)
     e1.record(stream)
     e1.synchronize()
     ens.sync()
@@ -426,18 +439,18 @@ def run_ensemble(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for v in views:
-        v.step(args.steps)   # returns when the member's steps are done
+        v.step(steps)   # returns when the member's steps are done
     ms_seq = (time.perf_counter() - t0) * 1e3
     line = {
-        "metric": "aggregate particle-steps/s (64-member ensemble)", "value": total * args.steps / (ms_ens / 1e3),
-        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_ens / args.steps,
+        "metric": "aggregate particle-steps/s (64-member ensemble)", "value": total * steps / (ms_ens / 1e3),
+        "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": ms_ens / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "ensemble of 64 members, particle counts log-uniform in [16384, 524288] (seed 7), "
                                "small-box atmosphere at fixed spacing, theta noise 0.1 K",
                    "members": len(members), "particles_total": total,
                    "particles_min": min(int(p.n_particles) for p in members),
                    "particles_max": max(int(p.n_particles) for p in members)},
-        "sequential": {"value": total * args.steps / (ms_seq / 1e3), "ms_per_step": ms_seq / args.steps,
+        "sequential": {"value": total * steps / (ms_seq / 1e3), "ms_per_step": ms_seq / steps,
                        "how": "each member's own graph-launched plain step; member k runs its K steps to "
                               "completion before member k+1 starts"},
         "speedup_vs_sequential": ms_seq / ms_ens,
@@ -447,15 +460,21 @@ def run_ensemble(args):
                                           for s in sorted(set(c[1] for c in chosen))},
                    "chosen_targets_per_thread_counts": {str(s): sum(1 for c in chosen if c[2] == s)
                                                         for s in sorted(set(c[2] for c in chosen))}},
-        "gpu_launches": args.steps * member_kernels,
+        "gpu_launches": steps * member_kernels,
         "clocks": clk,
     }
-    print(json.dumps(line))
     ens.close()
-    return 0
+    return line
 
 
 def run_adjoint(args):
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps(measure_adjoint(args.steps, args.warmup)))
+    return 0
+
+
+def measure_adjoint(K: int, warmup: int) -> dict:
     """Adjoint window on the 262,144-particle small-box workload: K plain
     steps against one window of K steps (forward with checkpoints every 10
     steps, backward with recompute) of the final cloud-water misfit."""
@@ -463,13 +482,11 @@ def run_adjoint(args):
     import sph_cuda_gb300 as sph
     from sph_cuda_gb300.adjoint import AdjointWindow, misfit, seeded_gaussians
 
-    torch.cuda.set_device(0)
     p = sph.preset("adjoint262k")
     sim = sph.Asph(p)
     sim.init()
     start = sim.snapshot()
-    K = args.steps
-    sim.step(max(args.warmup, 1))
+    sim.step(max(warmup, 1))
     # the plain steps from the window's start, three times; the fastest is the
     # denominator (the conservative choice for the ratio)
     t_plain = float("inf")
@@ -496,7 +513,7 @@ def run_adjoint(args):
     ratio = (t_fwd + t_bwd) / K / t_plain
     line = {
         "metric": "adjoint step time / forward step time (262,144 particles)", "value": ratio, "unit": "x",
-        "higher_is_better": False, "n_gpus": 1, "steps": K, "warmup": args.warmup, "dtype": "f32",
+        "higher_is_better": False, "n_gpus": 1, "steps": K, "warmup": warmup, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": "small-box atmosphere, 64 x 64 x 64 lattice, 50 x 50 x 100 cells, "
                                "checkpoints every 10 steps, misfit of final cloud water to 4 seeded Gaussians",
@@ -505,10 +522,34 @@ def run_adjoint(args):
         "backward_ms_per_step": t_bwd * 1e3 / K,
         "loss": L, "grad": {"max_abs_dtheta0": float(np.abs(dth).max()), "dalpha": da, "dbeta": db},
     }
-    print(json.dumps(line))
     win.close()
+    start.close()
     sim.close()
-    return 0
+    return line
+
+
+FORM_STEPS = {"ensemble64": 100, "adjoint262k": 100}
+
+
+def measure_forms() -> dict:
+    """The two other forms at their own configurations, after the headline's
+    timed region: the 64-member ensemble against its members run one after
+    another through the plain step, and the adjoint step against the plain
+    step (100-step window, checkpoints every 10 steps)."""
+    out = {}
+    e = measure_ensemble(FORM_STEPS["ensemble64"], 5)
+    out["ensemble64"] = {"value": e["value"], "unit": UNIT, "ms_per_step": e["ms_per_step"], "steps": e["steps"],
+                         "sequential_value": e["sequential"]["value"],
+                         "speedup_vs_sequential": e["speedup_vs_sequential"],
+                         "particles_total": e["config"]["particles_total"], "members": e["config"]["members"],
+                         "tuning_s": e["tuning"]["seconds"], "clocks": e["clocks"],
+                         "run": "python bench.py --workload ensemble64 --steps 100"}
+    a = measure_adjoint(FORM_STEPS["adjoint262k"], 5)
+    out["adjoint262k"] = {"adjoint_over_forward": a["value"], "plain_ms_per_step": a["plain_ms_per_step"],
+                          "window_forward_ms_per_step": a["window_forward_ms_per_step"],
+                          "backward_ms_per_step": a["backward_ms_per_step"], "steps": a["steps"],
+                          "run": "python bench.py --workload adjoint262k --steps 100"}
+    return out
 
 
 def parse_args(argv=None):
@@ -525,6 +566,8 @@ def parse_args(argv=None):
     ap.add_argument("--workload", default="bubble2m",
                     choices=["bubble2m", "bubble524k", "reference128", "large16m", "ensemble64", "adjoint262k"])
     ap.add_argument("--no-tune", action="store_true", help="ensemble64: skip the autotuner")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="bubble2m: skip the ensemble and adjoint measurements after the headline")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     return args
