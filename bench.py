@@ -239,7 +239,8 @@ def traffic_record(workload: str, steps_before: int, kernel: str):
         return None
     for rec in d.get("captures", []):
         if rec.get("steps_before") == steps_before and kernel in rec.get("bytes", {}):
-            return {"bytes": rec["bytes"][kernel], "source": d.get("source", path), "command": rec.get("command"),
+            return {"bytes": rec["bytes"][kernel], "source": "profiles/traffic_%s.json" % workload,
+                    "command": rec.get("command"), "steps_before": steps_before,
                     "companion": rec.get("companion", {}).get(kernel)}
     return None
 
@@ -371,7 +372,9 @@ def run_ours(args):
                          "frac": achieved / hbm, "peak_source": src,
                          "traffic": None if trec is None else trec["bytes"],
                          "traffic_source": ("no ncu capture of step %d of this workload" % (steps_before + 1))
-                         if trec is None else trec["source"],
+                         if trec is None else "%s: one launch of step %d (%s)" % (trec["source"], steps_before + 1,
+                                                                                 trec["command"]),
+                         "traffic_over_algorithmic": None if trec is None else trec["bytes"] / algo[dom],
                          "companion": None if trec is None else trec["companion"],
                          "kernel_ms": ph_ms, "kernel_ms_over": "the timed region's %d steps, replayed from a "
                                                                "snapshot with events between phases" % args.steps,

@@ -233,11 +233,19 @@ int asph_step_profiled(asph_ctx* ctx, int nsteps, float* phase_ms);
  * ASPH_OPT_TARGETS_PER_THREAD: targets each thread of the momentum pass
  * takes, 1, 2 (default) or 4, so that a warp covers 32, 64 or 128
  * consecutive targets (about 32 k / ppc cells, ppc = particles per cell);
- * 0 restores the default.  Results do not depend on it. */
+ * 0 restores the default.  Results do not depend on it.
+ * ASPH_OPT_SORT_AHEAD: 1 (default) = with a sort every step, a run of
+ * several steps (asph_step, asph_step_async with nsteps >= 2) sorts the
+ * next step's keys beside the current step's density and momentum passes,
+ * which neither read the sort's inputs later nor its outputs, and the next
+ * step's gather applies it; 0 = every step sorts at its start.  Results are
+ * bit-identical either way; between calls the context always holds the
+ * last applied sort. */
 #define ASPH_OPT_PAIR_PATH  1
 #define ASPH_OPT_PAIR_SHAPE 2
 #define ASPH_OPT_SORT_EVERY 3
 #define ASPH_OPT_TARGETS_PER_THREAD 4
+#define ASPH_OPT_SORT_AHEAD 5
 int asph_set_option(asph_ctx* ctx, int option, int value);
 int asph_get_option(asph_ctx* ctx, int option, int* value);
 

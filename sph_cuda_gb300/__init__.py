@@ -242,6 +242,17 @@ class Asph:
         """Momentum-pass targets per thread: 1, 2 or 4 (a warp covers 32 k targets)."""
         _check(self.lib.asph_set_option(self._ctx, abi.OPT_TARGETS_PER_THREAD, int(k)))
 
+    def sort_ahead(self) -> bool:
+        v = C.c_int()
+        _check(self.lib.asph_get_option(self._ctx, abi.OPT_SORT_AHEAD, C.byref(v)))
+        return bool(v.value)
+
+    def set_sort_ahead(self, on: bool) -> None:
+        """With a sort every step, runs of several steps sort the next step's
+        keys beside the current step's pair passes (on by default); results
+        are bit-identical either way."""
+        _check(self.lib.asph_set_option(self._ctx, abi.OPT_SORT_AHEAD, int(bool(on))))
+
     # ---- source-term hook ---------------------------------------------------------
     def enable_source(self, on: bool = True) -> None:
         """Per-particle additive tendencies of theta, qv, qc applied in every

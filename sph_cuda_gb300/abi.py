@@ -33,6 +33,7 @@ OPT_PAIR_PATH = 1
 OPT_PAIR_SHAPE = 2
 OPT_SORT_EVERY = 3
 OPT_TARGETS_PER_THREAD = 4
+OPT_SORT_AHEAD = 5
 NOALLOC_MAX_KEYS = 524288
 NBR_CAP = 192
 PHASES = ("table_clear", "sort", "gather_kick_drift", "density_eos", "momentum_integrate", "step")

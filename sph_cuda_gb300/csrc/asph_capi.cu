@@ -332,6 +332,9 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
         cudaError_t e = cudaStreamCreateWithFlags(&B.aux, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B.ev_fork, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B.ev_join, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&B.aux2, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B.ev_fork2, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B.ev_join2, cudaEventDisableTiming);
         if (e != cudaSuccess) {
             delete c;
             return fail(ASPH_ERR_CUDA, "stream create: %s", cudaGetErrorString(e));
@@ -347,6 +350,7 @@ extern "C" int asph_create(const AsphParams* p, void* stream, asph_ctx** out) {
         AL(B.pos[k], N * 16); AL(B.vel[k], N * 16); AL(B.thq[k], N * 16);
         AL(B.kbuf[k], N * 4); AL(B.vbuf[k], N * 4); AL(B.rain[k], C * 4);
     }
+    AL(B.skeys_ahead, N * 4); AL(B.perm_ahead, N * 4);
     AL(B.rp, N * 8); AL(B.acc, N * 16); AL(B.ms[0], N * 16); AL(B.ms[1], N * 16); AL(B.dthdt, N * 4); AL(B.kin, N * 4);
     AL(B.status, (size_t)B.npasses * B.ntiles * 256 * 8);
     AL(B.range, C * 8); AL(B.surf, N); AL(B.rain_delta, C * 4); AL(B.precip, (size_t)P.nxy * 4);
@@ -441,6 +445,9 @@ extern "C" int asph_set_option(asph_ctx* c, int option, int value) {
         if (value != 0 && value != 1 && value != 2 && value != 4)
             return fail(ASPH_ERR_ARG, "momentum targets per thread must be 1, 2 or 4 (0: default)");
         c->B.m_tpt = value;
+    } else if (option == ASPH_OPT_SORT_AHEAD) {
+        if (value != 0 && value != 1) return fail(ASPH_ERR_ARG, "sort ahead must be 0 or 1");
+        c->sort_ahead = value != 0;
     } else {
         return fail(ASPH_ERR_ARG, "unknown option %d", option);
     }
@@ -468,6 +475,10 @@ extern "C" int asph_get_option(asph_ctx* c, int option, int* value) {
     }
     if (option == ASPH_OPT_TARGETS_PER_THREAD) {
         *value = c->B.m_tpt > 0 ? c->B.m_tpt : 2;
+        return ASPH_OK;
+    }
+    if (option == ASPH_OPT_SORT_AHEAD) {
+        *value = c->sort_ahead ? 1 : 0;
         return ASPH_OK;
     }
     return fail(ASPH_ERR_ARG, "unknown option %d", option);
@@ -891,14 +902,22 @@ extern "C" int asph_cfl(asph_ctx* c) {
 }
 
 // One full step: sort (gated on the device) -> G -> D -> M(+rain,+CFL).
-void asph::enqueue_step(asph_ctx* c) {
+// In a run of steps with a sort every step, the next step's sort is forked
+// off after G (it needs G's keys of the drifted positions and the last
+// applied sort, and writes only its own buffers) and joined after M, so it
+// runs beside D and M; the next step's G applies it (StepKind).
+void asph::enqueue_step(asph_ctx* c, int kind) {
     const Phys& P = c->P;
     launch_sort_prep(P, c->B, 0, reads_rain(P) ? 1 : 0, c->stream);
-    launch_sort(P, c->B, 0, c->stream);
-    launch_gather(P, c->B, G_SORTED | G_INTEGRATE, c->stream);
+    if (kind == STEP_PLAIN || kind == STEP_FIRST) launch_sort(P, c->B, 0, c->stream);
+    launch_gather(P, c->B, G_SORTED | G_INTEGRATE | ((kind == STEP_MID || kind == STEP_LAST) ? G_AHEAD : 0),
+                  c->stream);
     c->B.pc ^= 1; c->B.vc ^= 1; c->B.qc ^= 1;
+    const bool ahead = kind == STEP_FIRST || kind == STEP_MID;
+    if (ahead) launch_sort_ahead(P, c->B, c->stream);
     launch_density(P, c->B, c->stream);
     launch_momentum(P, c->B, M_INTEGRATE | M_RAIN | M_CFL, 1, c->stream);
+    if (ahead) cudaStreamWaitEvent(c->stream, c->B.ev_join2, 0);
     c->B.vc ^= 1; c->B.rc ^= 1;
     c->lists_valid = true;
 }
@@ -945,13 +964,15 @@ extern "C" int asph_step_profiled(asph_ctx* c, int nsteps, float* phase_ms) {
 
 int asph::graph_slot(const Bufs& B) { return B.pc | (B.vc << 1) | (B.qc << 2) | (B.rc << 3); }
 
-// Capture the step that starts from the current ping-pong state into its
-// graph (the indices are left as they were); counts the graph's kernels.
-static int capture_step_graph(asph_ctx* c, int slot) {
+// Capture the step of `kind` that starts from the current ping-pong state
+// into its graph (the indices are left as they were); counts the graph's
+// kernels.
+static int capture_step_graph(asph_ctx* c, int kind) {
+    const int slot = kind * 16 + graph_slot(c->B);
     const Bufs saved = c->B;
     cudaGraph_t g = nullptr;
     CKR(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_step(c);
+    enqueue_step(c, kind);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     c->B = saved;
     if (e != cudaSuccess) return fail(ASPH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
@@ -968,19 +989,32 @@ static int capture_step_graph(asph_ctx* c, int slot) {
     if (e == cudaSuccess) e = cudaGraphInstantiate(&c->gexec[slot], g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(ASPH_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-    c->graph_kernels = kernels;
+    c->graph_kernels[kind] = kernels;
     return ASPH_OK;
 }
 
+// Whether a run of nsteps steps sorts ahead (a sort every step, the option
+// on, at least two steps).
+static bool runs_ahead(const asph_ctx* c, int nsteps) {
+    return c->sort_ahead && c->P.sort_every == 1 && nsteps >= 2;
+}
+
+static int step_kind(const asph_ctx* c, int k, int nsteps) {
+    if (!runs_ahead(c, nsteps)) return STEP_PLAIN;
+    return k == 0 ? STEP_FIRST : (k == nsteps - 1 ? STEP_LAST : STEP_MID);
+}
+
+// Kernel nodes per step of a long run: the middle steps' graph when the run
+// sorts ahead, else the plain step's.
 extern "C" int asph_step_kernels(asph_ctx* c, int* n) {
     if (!c || !n) return fail(ASPH_ERR_ARG, "NULL argument");
     if (!c->initialised) return fail(ASPH_ERR_STATE, "step_kernels before init/set_state");
-    const int slot = graph_slot(c->B);
-    if (!c->gexec[slot]) {
-        const int st = capture_step_graph(c, slot);
+    const int kind = step_kind(c, 1, 3);
+    if (!c->gexec[kind * 16 + graph_slot(c->B)]) {
+        const int st = capture_step_graph(c, kind);
         if (st) return st;
     }
-    *n = c->graph_kernels;
+    *n = c->graph_kernels[kind];
     return ASPH_OK;
 }
 
@@ -989,9 +1023,10 @@ extern "C" int asph_step_async(asph_ctx* c, int nsteps) {
     if (!c->initialised) return fail(ASPH_ERR_STATE, "step before init/set_state");
     ensure_spans(c);
     for (int k = 0; k < nsteps; ++k) {
-        const int slot = graph_slot(c->B);
+        const int kind = step_kind(c, k, nsteps);
+        const int slot = kind * 16 + graph_slot(c->B);
         if (!c->gexec[slot]) {
-            const int st = capture_step_graph(c, slot);
+            const int st = capture_step_graph(c, kind);
             if (st) return st;
         }
         CKR(cudaGraphLaunch(c->gexec[slot], c->stream));

@@ -17,9 +17,10 @@ struct asph_ctx {
     bool initialised = false;
     bool lists_valid = false;   // neighbour lists match the current positions
     bool spans_valid = false;   // brick spans match the sorted keys and the brick shape in use
-    // graphs keyed by the ping-pong state at the start of the step
-    cudaGraphExec_t gexec[16] = {};
-    int graph_kernels = 0;      // kernel nodes of a captured step graph
+    // step graphs keyed by kind (StepKind) x the ping-pong state at the start of the step
+    cudaGraphExec_t gexec[4 * 16] = {};
+    int graph_kernels[4] = {};  // kernel nodes of a captured step graph of each kind
+    bool sort_ahead = true;     // ASPH_OPT_SORT_AHEAD
     unsigned graph_epoch = 0;   // bumped whenever an option change drops the captured graphs
     // staging for host <-> device SoA copies (16 floats per particle)
     float* stage = nullptr;
@@ -59,6 +60,9 @@ struct asph_ctx {
         if (B.ev_fork) cudaEventDestroy(B.ev_fork);
         if (B.ev_join) cudaEventDestroy(B.ev_join);
         if (B.aux) cudaStreamDestroy(B.aux);
+        if (B.ev_fork2) cudaEventDestroy(B.ev_fork2);
+        if (B.ev_join2) cudaEventDestroy(B.ev_join2);
+        if (B.aux2) cudaStreamDestroy(B.aux2);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 };
@@ -69,9 +73,16 @@ int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
 // Wait for the context's stream and turn the device error word / CFL abort
 // flag into a status.
 int sync_status(asph_ctx* c);
+// Kinds of captured step.  STEP_PLAIN sorts at its start.  In a run of
+// several steps with a sort every step, the first step (STEP_FIRST) sorts at
+// its start and also sorts the next step's keys beside its pair passes, the
+// middle steps (STEP_MID) apply the sort run ahead and run the next one, and
+// the last (STEP_LAST) applies the sort run ahead and runs none, so that
+// between calls the context holds the last applied sort.
+enum StepKind : int { STEP_PLAIN = 0, STEP_FIRST = 1, STEP_MID = 2, STEP_LAST = 3 };
 // Enqueue one full step (sort, gather/kick/drift/flux, density, momentum)
 // on the context's stream and advance the ping-pong indices.
-void enqueue_step(asph_ctx* c);
+void enqueue_step(asph_ctx* c, int kind = STEP_PLAIN);
 // Graph key of the ping-pong state at the start of a step.
 int graph_slot(const Bufs& B);
 void apply_pending_clamp(asph_ctx* c);

@@ -57,6 +57,11 @@ struct Bufs {
     uint32_t* vbuf[2];  // radix ping-pong values
     uint32_t* skeys;    // sorted keys of the last sort (points into kbuf)
     uint32_t* perm;     // permutation of the last sort (points into vbuf)
+    // the next step's sort, run ahead beside this step's pair passes (see
+    // launch_sort_ahead); the next gather applies it and copies it into
+    // skeys/perm
+    uint32_t* skeys_ahead;
+    uint32_t* perm_ahead;
     uint64_t* status;   // look-back words [pass][tile][digit]
     // incremental sort: unchanged indices, changed keys/indices (ping-pong),
     // per-block counts, the changed-key sort's look-back words
@@ -86,6 +91,8 @@ struct Bufs {
     int m_tpt;          // targets per thread of the momentum pass (1, 2 or 4; 0: the default, 2)
     cudaStream_t aux;   // second stream: the full sort runs beside the incremental one (a graph branch)
     cudaEvent_t ev_fork, ev_join;
+    cudaStream_t aux2;  // third stream: the next step's sort beside this step's pair passes
+    cudaEvent_t ev_fork2, ev_join2;
     float4* src;        // source-term hook: per-particle tendencies (theta, qv, qc), NULL when off
     float4* src_tmp;    // the tendencies in the order of the current step (written by the gather)
 };
@@ -95,6 +102,7 @@ enum : int {
     G_SORTED    = 1,    // gather through the permutation when a sort ran
     G_INTEGRATE = 2,    // half kick + drift + surface flux
     G_FORCE     = 4,    // the sort ran unconditionally (granular call)
+    G_AHEAD     = 8,    // apply the sort run ahead (skeys_ahead/perm_ahead) and copy it into skeys/perm
 };
 // Mode bits of the momentum pass.
 enum : int {
@@ -113,6 +121,14 @@ void launch_init(const Phys& P, const Bufs& B, const float* bub, int nbub, int i
 void launch_keys(const Phys& P, const Bufs& B, cudaStream_t s);
 void launch_sort_prep(const Phys& P, const Bufs& B, int force, int clear_delta, cudaStream_t s);
 void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s);
+// The next step's sort, enqueued right after this step's gather wrote the
+// keys of the drifted positions: the same stable sort of the same keys, into
+// skeys_ahead/perm_ahead, on its own stream branch so that it runs beside
+// the density and momentum passes (which read neither its inputs' future
+// values nor its outputs).  It runs whatever the step gating says; only a
+// sort-every-step cadence may use it, and the next gather decides as
+// always whether a sort is applied.
+void launch_sort_ahead(const Phys& P, Bufs& B, cudaStream_t s);
 // Sizes of the incremental sort's buffers for N particles.
 void sort_inc_sizes(int N, int* max_keys, int* tiles, int* blocks);
 void launch_gather(const Phys& P, const Bufs& B, int mode, cudaStream_t s);

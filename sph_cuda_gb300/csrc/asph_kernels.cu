@@ -106,6 +106,7 @@ struct GArgs {
     const float2* rp;
     const float4* acc;
     const uint32_t *perm, *skeys;
+    uint32_t *perm_out, *skeys_out;   // non-NULL: the sort was run ahead; copy it into the last-sort buffers
     int2* range;
     int2* spans;         // brick spans of the density pass by Morton id (NULL: global path) ...
     int span_shift;      // ... a brick's id is its keys >> span_shift
@@ -142,6 +143,10 @@ __global__ __launch_bounds__(TPB) void k_gather(const __grid_constant__ Phys P, 
             // keys decode to cells inside the grid; the bounds test only guards
             // against a sort that gave up (error word set)
             const uint32_t kc = A.skeys[i];
+            if (A.skeys_out) {
+                A.skeys_out[i] = kc;
+                A.perm_out[i] = (uint32_t)s;
+            }
             const int c = cid_of_key(P, kc);
             const bool cin = (unsigned)c < (unsigned)P.ncell;
             if (i == 0) {
@@ -378,7 +383,12 @@ void launch_gather(const Phys& P, const Bufs& B, int mode, cudaStream_t s) {
     GArgs A;
     A.pos_src = B.pos[B.pc]; A.vel_src = B.vel[B.vc]; A.thq_src = B.thq[B.qc];
     A.pos_dst = B.pos[1 - B.pc]; A.vel_dst = B.vel[1 - B.vc]; A.thq_dst = B.thq[1 - B.qc];
-    A.rp = B.rp; A.acc = B.acc; A.perm = B.perm; A.skeys = B.skeys; A.range = B.range;
+    A.rp = B.rp; A.acc = B.acc; A.range = B.range;
+    if (mode & G_AHEAD) {
+        A.perm = B.perm_ahead; A.skeys = B.skeys_ahead; A.perm_out = B.perm; A.skeys_out = B.skeys;
+    } else {
+        A.perm = B.perm; A.skeys = B.skeys; A.perm_out = nullptr; A.skeys_out = nullptr;
+    }
     A.span_shift = pair_span_shift(P, B);
     A.spans = A.span_shift >= 0 ? B.spans : nullptr;
     A.surf = B.surf; A.kin = B.kin; A.ctl = B.ctl;

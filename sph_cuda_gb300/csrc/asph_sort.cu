@@ -29,6 +29,12 @@ constexpr uint64_t FLAG_AGG = 1ull << 30;
 constexpr uint64_t FLAG_PRE = 2ull << 30;
 constexpr uint64_t CNT_MASK = (1ull << 30) - 1;
 
+// Gate of a sort launch (`force`): 0 the step's gating (the control
+// block's do_sort, nothing after an abort), 1 a forced full sort (granular
+// call), GATE_AHEAD the next step's sort run ahead, which always runs (the
+// gather that would apply it still follows the step's gating).
+constexpr int GATE_AHEAD = 2;
+
 __device__ __forceinline__ bool sort_runs(const DevCtl* ctl, int force) {
     return force || (ctl->do_sort && !ctl->aborted);
 }
@@ -37,8 +43,9 @@ __device__ __forceinline__ bool sort_runs(const DevCtl* ctl, int force) {
 // changed since the last sort (incremental path).  The step launches both;
 // the control block decides which one works.
 __device__ __forceinline__ bool lane_runs(const DevCtl* ctl, int force, int sort_lane) {
-    if (sort_lane == 0) return force || (ctl->do_sort && !ctl->aborted && !ctl->inc_on);
-    return !force && ctl->do_sort && !ctl->aborted && ctl->inc_on;
+    const bool go = force == GATE_AHEAD || (ctl->do_sort && !ctl->aborted);
+    if (sort_lane == 0) return force == 1 || (go && !ctl->inc_on);
+    return force != 1 && go && ctl->inc_on;
 }
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -264,13 +271,16 @@ constexpr int INC_TPB = 256;
 constexpr int INC_CHUNK = INC_TPB * 8;   // keys per compaction block
 constexpr int MERGE_ITEMS = 8;           // outputs per merge thread
 
-__device__ __forceinline__ bool inc_step_sorts(const DevCtl* ctl) { return ctl->do_sort && !ctl->aborted; }
+__device__ __forceinline__ bool inc_step_sorts(const DevCtl* ctl, int gate) {
+    return gate == GATE_AHEAD || (ctl->do_sort && !ctl->aborted);
+}
 }  // namespace
 
 __global__ __launch_bounds__(INC_TPB) void k_inc_count(const uint32_t* __restrict__ kin,
                                                        const uint32_t* __restrict__ sprev, int N,
-                                                       uint32_t* __restrict__ cnt, const DevCtl* __restrict__ ctl) {
-    if (!inc_step_sorts(ctl)) return;
+                                                       uint32_t* __restrict__ cnt, const DevCtl* __restrict__ ctl,
+                                                       int gate) {
+    if (!inc_step_sorts(ctl, gate)) return;
     __shared__ uint32_t s_red[INC_TPB / 32];
     const int base = blockIdx.x * INC_CHUNK;
     const int end = min(base + INC_CHUNK, N);
@@ -288,10 +298,11 @@ __global__ __launch_bounds__(INC_TPB) void k_inc_count(const uint32_t* __restric
 }
 
 // One block: block counts -> exclusive offsets; decides the path.
-__global__ void k_inc_scan(uint32_t* __restrict__ cnt, int nblocks, int inc_max, DevCtl* __restrict__ ctl) {
+__global__ void k_inc_scan(uint32_t* __restrict__ cnt, int nblocks, int inc_max, DevCtl* __restrict__ ctl,
+                           int gate) {
     __shared__ uint32_t s_warp[32];
     __shared__ uint32_t s_carry;
-    if (!inc_step_sorts(ctl)) {
+    if (!inc_step_sorts(ctl, gate)) {
         if (threadIdx.x == 0) ctl->inc_on = 0;
         return;
     }
@@ -341,8 +352,9 @@ __global__ __launch_bounds__(INC_TPB) void k_inc_split(const uint32_t* __restric
                                                        const uint32_t* __restrict__ sprev, int N,
                                                        const uint32_t* __restrict__ off, uint32_t* __restrict__ uidx,
                                                        uint32_t* __restrict__ ukey, uint32_t* __restrict__ ck,
-                                                       uint32_t* __restrict__ ci, const DevCtl* __restrict__ ctl) {
-    if (!inc_step_sorts(ctl) || !ctl->inc_on) return;
+                                                       uint32_t* __restrict__ ci, const DevCtl* __restrict__ ctl,
+                                                       int gate) {
+    if (!inc_step_sorts(ctl, gate) || !ctl->inc_on) return;
     __shared__ uint32_t s_warp[INC_TPB / 32];
     const int base = blockIdx.x * INC_CHUNK;
     uint32_t oc = off[blockIdx.x];          // changed before this block
@@ -391,8 +403,8 @@ __global__ __launch_bounds__(INC_TPB) void k_inc_merge(const uint32_t* __restric
                                                        const uint32_t* __restrict__ ck,
                                                        const uint32_t* __restrict__ ci, int N,
                                                        uint32_t* __restrict__ skeys, uint32_t* __restrict__ perm,
-                                                       const DevCtl* __restrict__ ctl) {
-    if (!inc_step_sorts(ctl) || !ctl->inc_on) return;
+                                                       const DevCtl* __restrict__ ctl, int gate) {
+    if (!inc_step_sorts(ctl, gate) || !ctl->inc_on) return;
     __shared__ uint32_t s_k[INC_TPB * MERGE_ITEMS], s_i[INC_TPB * MERGE_ITEMS];
     const int m = (int)ctl->inc_m, nu = N - m;
     const long long t0 = (long long)blockIdx.x * INC_TPB * MERGE_ITEMS;   // the block's first output
@@ -453,8 +465,8 @@ void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s) {
     const bool inc = !force && B.inc_u;
     if (inc) {
         // decide the path: count the changed keys (lane 1 runs when few changed)
-        k_inc_count<<<B.inc_blocks, INC_TPB, 0, s>>>(B.kin, B.skeys, P.N, B.inc_cnt, B.ctl);
-        k_inc_scan<<<1, 1024, 0, s>>>(B.inc_cnt, B.inc_blocks, B.inc_max, B.ctl);
+        k_inc_count<<<B.inc_blocks, INC_TPB, 0, s>>>(B.kin, B.skeys, P.N, B.inc_cnt, B.ctl, 0);
+        k_inc_scan<<<1, 1024, 0, s>>>(B.inc_cnt, B.inc_blocks, B.inc_max, B.ctl, 0);
     }
     // Exactly one of the two sorts does work; the device flag decides.  With
     // both, the full sort runs on the second stream (in a captured step, a
@@ -478,7 +490,7 @@ void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s) {
     if (fork) cudaEventRecord(B.ev_join, B.aux);
     if (inc) {
         k_inc_split<<<B.inc_blocks, INC_TPB, 0, s>>>(B.kin, B.skeys, P.N, B.inc_cnt, B.inc_u, B.inc_uk, B.inc_k[0],
-                                                     B.inc_i[0] + 0, B.ctl);
+                                                     B.inc_i[0] + 0, B.ctl, 0);
         // the changed keys: stable radix sort of (key, index), lane 1
         int ib = (B.inc_max + TPB * 8 - 1) / (TPB * 8);
         ib = ib < 1 ? 1 : (ib > 152 * 8 ? 152 * 8 : ib);
@@ -494,9 +506,74 @@ void launch_sort(const Phys& P, Bufs& B, int force, cudaStream_t s) {
             vi = vo;
         }
         const int mb = (P.N + INC_TPB * MERGE_ITEMS - 1) / (INC_TPB * MERGE_ITEMS);
-        k_inc_merge<<<mb, INC_TPB, 0, s>>>(B.inc_u, B.inc_uk, ki, vi, P.N, B.skeys, B.perm, B.ctl);
+        k_inc_merge<<<mb, INC_TPB, 0, s>>>(B.inc_u, B.inc_uk, ki, vi, P.N, B.skeys, B.perm, B.ctl, 0);
     }
     if (fork) cudaStreamWaitEvent(s, B.ev_join, 0);
+}
+
+// Resets the full sort's histograms and tile counters and opens a new
+// look-back epoch, for a sort run ahead (k_sort_prep does it for the step's
+// own sort, together with the table clear that must wait for the step's
+// pair passes).
+__global__ void k_sort_state(DevCtl* __restrict__ ctl) {
+    for (int i = threadIdx.x; i < MAX_PASSES * 256; i += blockDim.x) (&ctl->hist[0][0])[i] = 0u;
+    if (threadIdx.x < MAX_PASSES) ctl->tile_ctr[threadIdx.x] = 0u;
+    if (threadIdx.x == 0) ctl->epoch += 1u;
+}
+
+void launch_sort_ahead(const Phys& P, Bufs& B, cudaStream_t s) {
+    if (P.N <= 0) return;
+    // branch off the caller's stream; the caller's later work does not wait
+    // for it until the join at the end
+    cudaEventRecord(B.ev_fork2, s);
+    cudaStreamWaitEvent(B.aux2, B.ev_fork2, 0);
+    cudaStream_t a = B.aux2;
+    k_sort_state<<<1, 256, 0, a>>>(B.ctl);
+    k_inc_count<<<B.inc_blocks, INC_TPB, 0, a>>>(B.kin, B.skeys, P.N, B.inc_cnt, B.ctl, GATE_AHEAD);
+    k_inc_scan<<<1, 1024, 0, a>>>(B.inc_cnt, B.inc_blocks, B.inc_max, B.ctl, GATE_AHEAD);
+    // the full sort (when too many keys changed) on a branch of its own; its
+    // passes alternate between skeys_ahead and the key buffer that is not
+    // skeys, ending in skeys_ahead, so the last applied sort stays intact
+    cudaEventRecord(B.ev_fork, a);
+    cudaStreamWaitEvent(B.aux, B.ev_fork, 0);
+    int hb = (P.N + TPB * 8 - 1) / (TPB * 8);
+    hb = hb > 152 * 8 ? 152 * 8 : hb;
+    k_hist<<<hb, SORT_TPB, 0, B.aux>>>(B.kin, P.N, B.npasses, B.ctl, GATE_AHEAD, 0);
+    uint32_t* kscr = B.kbuf[B.skeys == B.kbuf[0] ? 1 : 0];
+    uint32_t* vscr = B.vbuf[B.perm == B.vbuf[0] ? 1 : 0];
+    const uint32_t* ki = B.kin;
+    const uint32_t* vi = nullptr;
+    for (int p = 0; p < B.npasses; ++p) {
+        const bool last_parity = ((B.npasses - 1 - p) & 1) == 0;
+        uint32_t* ko = last_parity ? B.skeys_ahead : kscr;
+        uint32_t* vo = last_parity ? B.perm_ahead : vscr;
+        k_radix_pass<<<B.ntiles, SORT_TPB, 0, B.aux>>>(ki, vi, ko, vo, B.status, P.N, B.ntiles, p, B.ctl,
+                                                       GATE_AHEAD, 0);
+        ki = ko;
+        vi = vo;
+    }
+    cudaEventRecord(B.ev_join, B.aux);
+    // the incremental sort
+    k_inc_split<<<B.inc_blocks, INC_TPB, 0, a>>>(B.kin, B.skeys, P.N, B.inc_cnt, B.inc_u, B.inc_uk, B.inc_k[0],
+                                                 B.inc_i[0], B.ctl, GATE_AHEAD);
+    int ib = (B.inc_max + TPB * 8 - 1) / (TPB * 8);
+    ib = ib < 1 ? 1 : (ib > 152 * 8 ? 152 * 8 : ib);
+    k_hist<<<ib, SORT_TPB, 0, a>>>(B.inc_k[0], B.inc_max, B.npasses, B.ctl, GATE_AHEAD, 1);
+    const uint32_t* ik = B.inc_k[0];
+    const uint32_t* iv = B.inc_i[0];
+    for (int p = 0; p < B.npasses; ++p) {
+        uint32_t* ko = B.inc_k[(p + 1) & 1];
+        uint32_t* vo = B.inc_i[(p + 1) & 1];
+        k_radix_pass<<<B.inc_tiles, SORT_TPB, 0, a>>>(ik, iv, ko, vo, B.inc_status, B.inc_max, B.inc_tiles, p,
+                                                      B.ctl, GATE_AHEAD, 1);
+        ik = ko;
+        iv = vo;
+    }
+    const int mb = (P.N + INC_TPB * MERGE_ITEMS - 1) / (INC_TPB * MERGE_ITEMS);
+    k_inc_merge<<<mb, INC_TPB, 0, a>>>(B.inc_u, B.inc_uk, ik, iv, P.N, B.skeys_ahead, B.perm_ahead, B.ctl,
+                                       GATE_AHEAD);
+    cudaStreamWaitEvent(a, B.ev_join, 0);
+    cudaEventRecord(B.ev_join2, a);
 }
 
 }  // namespace asph

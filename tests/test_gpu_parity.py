@@ -549,15 +549,76 @@ def test_brick_spans_follow_shape_changes_and_restores():
 
 
 def test_step_kernels_count_the_step_graph():
-    """The kernel launches of a plain step, read from the captured graph: the sort preparation,
+    """The kernel launches of a step, read from the captured graph: the sort preparation,
     both sorts (the full one a graph branch; a histogram and 3 passes each at 18-bit keys, plus
     the incremental sort's count, scan, split and merge), the gather, the density pass and its
-    deferred kernel, and momentum."""
+    deferred kernel, and momentum.  A step in the middle of a run that sorts ahead has the same
+    kernels plus the reset of the sort's histograms that the preparation does otherwise."""
     p = small_config(lat=(24, 24, 24), grid=(30, 30, 60), box=(6000.0, 6000.0, 3000.0), sort_every=1)
     sim = Asph(p)
     sim.init()
+    passes = (3 * 6 + 7) // 8      # 6 bits per axis at 60 cells
+    plain = 1 + (1 + passes) + (4 + 1 + passes) + 1 + 2 + 1
     n0 = sim.step_kernels()        # captured without running
     sim.step(3)
-    passes = (3 * 6 + 7) // 8      # 6 bits per axis at 60 cells
-    assert n0 == sim.step_kernels() == 1 + (1 + passes) + (4 + 1 + passes) + 1 + 2 + 1
+    assert n0 == sim.step_kernels() == plain + 1
+    sim.set_sort_ahead(False)
+    assert sim.step_kernels() == plain
     sim.close()
+
+
+def _sort_state(sim):
+    g = sim.get_sort()
+    return {k: np.asarray(v).copy() for k, v in g.items()}
+
+
+def test_sort_ahead_equals_sorting_at_each_step():
+    """With a sort every step, runs of steps sort the next step's keys beside the current
+    step's pair passes and the next gather applies them (ASPH_OPT_SORT_AHEAD).  The states,
+    the last applied sort (keys, permutation, sorted keys, cell table) and the control block
+    equal those of the same steps sorting at their start, bit for bit, over calls of 1, 2 and
+    7 steps, with the source-term hook on; and after a CFL abort in the middle of a run."""
+    p = small_config(lat=(24, 24, 24), grid=(30, 30, 60), box=(6000.0, 6000.0, 3000.0), sort_every=1)
+    sims = []
+    for ahead in (True, False):
+        sim = Asph(p)
+        sim.init()
+        sim.set_sort_ahead(ahead)
+        sim.enable_source(True)
+        n = int(p.n_particles)
+        rng = np.random.default_rng(3)
+        sim.set_source(rng.normal(0, 1e-3, n).astype(np.float32), np.zeros(n, np.float32), np.zeros(n, np.float32))
+        sims.append(sim)
+    assert sims[0].sort_ahead() and not sims[1].sort_ahead()
+    for n in (1, 2, 7):
+        for sim in sims:
+            sim.step(n)
+        sa, sb = sims[0].get_state(), sims[1].get_state()
+        for k in sa:
+            assert np.array_equal(sa[k], sb[k]), (n, k)
+        ga, gb = _sort_state(sims[0]), _sort_state(sims[1])
+        for k in ga:
+            assert np.array_equal(ga[k], gb[k]), (n, k)
+        ca, cb = sims[0].control(), sims[1].control()
+        for k in ("dt", "simt", "step", "sort_count", "umax", "wmax", "aborted", "error"):
+            assert ca[k] == cb[k], (n, k)
+        assert np.array_equal(sims[0].get_rain()[0], sims[1].get_rain()[0])
+    for sim in sims:
+        sim.close()
+    # an abort at the first step of a 3-step run: both keep the sort the frozen state was built with
+    ps = reference_geometry(16, 16, 8, strict_cfl=1, sort_every=1)
+    s = random_state(ps, 8, "jitter", speed=3000.0)
+    out = []
+    for ahead in (True, False):
+        sim = _ctx(ps, s)
+        sim.set_sort_ahead(ahead)
+        with pytest.raises(AsphError) as e:
+            sim.step(3)
+        assert e.value.status == abi.ASPH_ERR_CFL_ABORT
+        out.append((sim.get_state(), _sort_state(sim), sim.control()))
+        sim.close()
+    for k in out[0][0]:
+        assert np.array_equal(out[0][0][k], out[1][0][k]), k
+    for k in out[0][1]:
+        assert np.array_equal(out[0][1][k], out[1][1][k]), k
+    assert out[0][2]["step"] == out[1][2]["step"] == 1
