@@ -474,7 +474,7 @@ extern "C" int asph_get_option(asph_ctx* c, int option, int* value) {
         return ASPH_OK;
     }
     if (option == ASPH_OPT_TARGETS_PER_THREAD) {
-        *value = c->B.m_tpt > 0 ? c->B.m_tpt : 2;
+        *value = momentum_tpt(c->B);
         return ASPH_OK;
     }
     if (option == ASPH_OPT_SORT_AHEAD) {

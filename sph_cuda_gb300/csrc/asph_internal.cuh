@@ -134,6 +134,8 @@ void sort_inc_sizes(int N, int* max_keys, int* tiles, int* blocks);
 void launch_gather(const Phys& P, const Bufs& B, int mode, cudaStream_t s);
 void launch_density(const Phys& P, const Bufs& B, cudaStream_t s);
 void launch_momentum(const Phys& P, const Bufs& B, int mode, int use_lists, cudaStream_t s);
+// Targets per thread the momentum pass uses (the option, else the default).
+int momentum_tpt(const Bufs& B);
 void launch_rain(const Phys& P, const Bufs& B, cudaStream_t s);
 // Brick shape index the density pass uses (-1: per-target global path),
 // the number of shapes, and whether shape k suits the grid and density.
