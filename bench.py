@@ -225,11 +225,12 @@ def reference_gpu(args, ours_value: float):
             "clocks": clk}
 
 
-def traffic_record(workload: str, steps_before: int, kernel: str):
-    """DRAM bytes of one launch of `kernel` captured by ncu in exactly the
-    state the line's per-kernel times cover: profiles/traffic_<workload>.json
-    holds captures keyed by the number of steps completed before the captured
-    launch.  No capture for this state: None (the line says so)."""
+def traffic_record(workload: str, steps_before: int, steps: int, kernel: str):
+    """DRAM bytes of one launch of `kernel` captured by ncu in the state the
+    line's per-kernel times cover: profiles/traffic_<workload>.json holds
+    captures keyed by the number of steps completed before the captured
+    launch, each standing for a timed region of at most `max_steps` steps
+    from there.  No capture for this state: None (the line says so)."""
     path = os.path.join(ROOT, "profiles", "traffic_%s.json" % workload)
     if not os.path.exists(path):
         return None
@@ -238,7 +239,8 @@ def traffic_record(workload: str, steps_before: int, kernel: str):
     except Exception:
         return None
     for rec in d.get("captures", []):
-        if rec.get("steps_before") == steps_before and kernel in rec.get("bytes", {}):
+        if (rec.get("steps_before") == steps_before and steps <= rec.get("max_steps", 1)
+                and kernel in rec.get("bytes", {})):
             return {"bytes": rec["bytes"][kernel], "source": "profiles/traffic_%s.json" % workload,
                     "command": rec.get("command"), "steps_before": steps_before,
                     "companion": rec.get("companion", {}).get(kernel)}
@@ -328,7 +330,7 @@ def run_ours(args):
     achieved = algo[dom] / (ph_ms[dom] / 1e3) / 1e9
     # DRAM traffic of the dominant kernel from an ncu capture of the first
     # timed step of this same command (profiles/traffic_<workload>.json)
-    trec = traffic_record(args.workload, steps_before, dom)
+    trec = traffic_record(args.workload, steps_before, args.steps, dom)
 
     # end to end through the C ABI with pinned host buffers: per step the
     # persistent state goes host->device, one step runs, the state comes back
@@ -371,7 +373,8 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_source": src,
                          "traffic": None if trec is None else trec["bytes"],
-                         "traffic_source": ("no ncu capture of step %d of this workload" % (steps_before + 1))
+                         "traffic_source": ("no ncu capture of steps %d-%d of this workload"
+                                            % (steps_before + 1, steps_before + args.steps))
                          if trec is None else "%s: one launch of step %d (%s)" % (trec["source"], steps_before + 1,
                                                                                  trec["command"]),
                          "traffic_over_algorithmic": None if trec is None else trec["bytes"] / algo[dom],

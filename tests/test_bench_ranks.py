@@ -113,3 +113,15 @@ def test_other_workloads_and_options():
     a = bench.parse_args([])
     assert a.steps == 500 and a.advance == 0 and a.workload == "bubble2m"   # the configuration's 500 steps
     assert bench.parse_args(["--advance", "500"]).advance == 500
+
+
+def test_traffic_is_taken_only_from_a_capture_of_the_timed_state():
+    """The roofline's DRAM traffic comes from an ncu capture of the state the
+    line times: the first timed step after the warm-up, for a timed region
+    short enough that the state does not drift from it."""
+    r = bench.traffic_record("bubble2m", 5, 20, "density_eos")
+    assert r is not None and r["steps_before"] == 5 and r["bytes"] > 48 * 2097152
+    assert bench.traffic_record("bubble2m", 5, 500, "density_eos") is None     # 500 steps develop the bubbles
+    assert bench.traffic_record("bubble2m", 3, 20, "density_eos") is None      # another state
+    assert bench.traffic_record("bubble2m", 503, 2, "density_eos")["bytes"] > r["bytes"]
+    assert bench.traffic_record("large16m", 5, 20, "density_eos") is None      # no capture of that workload
