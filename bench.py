@@ -152,6 +152,8 @@ def workload_string(name: str) -> str:
             "bubble524k": "moist bubble, 524,288 particles, 66x66x200 cells, sort every step",
             "reference128": "the reference's own geometry and init, 128x128x128 cells, dt 0.25 s, "
                             "sort every step",
+            "large2m": "the large run's 8:1 cells and physics on a 20 x 20 x 5 km box, 2,097,152 particles, "
+                       "125x125x250 cells (h 160 m x 20 m), sort every step",
             "large16m": "large anisotropic run, 16,777,216 particles, 250x250x500 cells (h 160 m x 20 m), "
                         "95% RH boundary layer, theta noise 0.2 K, sort every step"}[name]
 
@@ -253,10 +255,20 @@ def workload_params(name: str):
     (64 x 64 x 128 lattice, 66 x 66 x 200 cells) for profiler captures.
     reference128: the reference's own configuration at --nx --ny --nz 128 and
     --dt 0.25 with a sort every step (what oracle/time_reference.py native runs).
-    large16m: the 16,777,216-particle anisotropic run (40 x 40 x 10 km, 8:1)."""
+    large16m: the 16,777,216-particle anisotropic run (40 x 40 x 10 km, 8:1).
+    large2m: its cells, lattice spacing and physics at 2,097,152 particles (a
+    20 x 20 x 5 km box: 128^3 lattice, 125 x 125 x 250 cells) for profiler
+    captures of the 8:1 kernels."""
     import sph_cuda_gb300 as sph
     if name == "large16m":
         return sph.preset("large16m")
+    if name == "large2m":
+        p = sph.preset("large16m")
+        p.nx = p.ny = 125
+        p.nz = 250
+        p.lat_nx = p.lat_ny = p.lat_nz = 128
+        p.n_particles = 128 ** 3
+        return p
     if name == "reference128":
         p = sph.preset("reference", 128, 128, 128)
         p.sort_every = 1
@@ -570,7 +582,8 @@ def parse_args(argv=None):
     ap.add_argument("--advance", type=int, default=0,
                     help="untimed steps after init, before warm-up (profile a developed state)")
     ap.add_argument("--workload", default="bubble2m",
-                    choices=["bubble2m", "bubble524k", "reference128", "large16m", "ensemble64", "adjoint262k"])
+                    choices=["bubble2m", "bubble524k", "reference128", "large16m", "large2m", "ensemble64",
+                             "adjoint262k"])
     ap.add_argument("--no-tune", action="store_true", help="ensemble64: skip the autotuner")
     ap.add_argument("--no-forms", action="store_true",
                     help="bubble2m: skip the ensemble and adjoint measurements after the headline")

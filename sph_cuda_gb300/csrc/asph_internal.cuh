@@ -31,7 +31,6 @@ struct DevCtl {
     unsigned split_n;          // brick regions split into halves in the running density pass
     unsigned split_last;       // ... in the last density pass
     unsigned gmax[3];          // float bits of |u|,|v|,|w| maxima (atomicMax)
-    unsigned done;             // finished-block counter of the momentum pass
     unsigned epoch;            // radix look-back epoch
     unsigned hist[MAX_PASSES][256];
     unsigned tile_ctr[MAX_PASSES];
@@ -108,7 +107,7 @@ enum : int {
 enum : int {
     M_INTEGRATE = 1,    // theta update, second half kick, sponge, velocity maxima
     M_RAIN      = 2,    // rain sedimentation blocks appended to the grid
-    M_CFL       = 4,    // last block runs the CFL control
+    M_CFL       = 4,    // the CFL control follows (a one-block kernel)
 };
 
 // Record a failure for asph_last_error() (asph_capi.cu); returns `code`.

@@ -51,7 +51,11 @@ constexpr int DLIST = 30;        // most queued accepted candidates per thread (
 // 2M from init: 0.298 / 0.260 / 0.257 / 0.271 ms at 32 / 64 / 128 / 256).
 constexpr int M_TPB = 128;
 constexpr int M_MINB = 1024 / M_TPB;                     // resident blocks that keep 64 registers
-constexpr int M_RAIN_CELLS = 256 / M_TPB;                // rain cells per thread of a rain block
+// Rain cells per thread of a rain block: 1,024 cells a block, so that the
+// rain advection adds few blocks (and few finished-block atomics) to the
+// pass (momentum at 2M from init: 0.262 / 0.245 / 0.256 ms at 256 / 1,024 /
+// 4,096 cells a block).
+constexpr int M_RAIN_CELLS = 8;
 constexpr int M_TPT = 2;         // default targets per thread of the momentum pass (1, 2 or 4 per launch)
 
 template <int BX, int BY, int BZ, int H>
@@ -660,7 +664,8 @@ struct MArgs {
     float* rain_out;
     float* precip;
     DevCtl* ctl;
-    int part_blocks;       // blocks of particle work; the rest advect rain
+    int part_blocks;       // chunks of particle work (TPT x M_TPB targets each) ...
+    int rain_blocks;       // ... then chunks of rain cells (M_RAIN_CELLS x M_TPB each)
 };
 
 // Out of line: targets without a usable neighbour list come here.
@@ -677,82 +682,92 @@ __device__ __noinline__ MSum momentum_target_global(const Phys& P, const MArgs& 
     return s;
 }
 
+// The TPT x M_TPB targets of particle chunk `ch`: the lanes of warp w on
+// targets w * 32 * TPT + lane + 32 r, so that a warp waits on the longest sum
+// of its lanes' lists rather than on the longest list of each round; a warp
+// covers 32 TPT consecutive targets, about 32 TPT / ppc cells.
+template <int TPT>
+__device__ __forceinline__ void momentum_chunk(const Phys& P, const MArgs& A, int mode, int ch, bool aborted,
+                                               float dt, float3& m) {
+    const int tbase = ch * (M_TPB * TPT) + (threadIdx.x >> 5) * (32 * TPT) + (threadIdx.x & 31);
+    for (int r = 0; r < TPT; ++r) {
+        const int i = tbase + 32 * r;
+        if (i >= P.N) continue;
+        if (aborted) {
+            if (mode & M_INTEGRATE) A.out.vel_out[i] = A.vel[i];
+            continue;
+        }
+        // (x, y, z, p') and (u, v, w, rho): packed by the density pass
+        // when the lists are current, else from the state buffers
+        float4 a, b;
+        if (A.use_lists) {
+            a = A.ms0[i];
+            b = A.ms1[i];
+        } else {
+            const float4 p = A.pos[i], v = A.vel[i];
+            const float2 rr = A.rp[i];
+            a = make_float4(p.x, p.y, p.z, rr.y);
+            b = make_float4(v.x, v.y, v.z, rr.x);
+        }
+        MTarget T;
+        T.x = a.x; T.y = a.y; T.z = a.z;
+        T.u = b.x; T.v = b.y; T.w = b.z;
+        T.rhoi = fmaxf(b.w, 1e-3f);
+        T.irhoi = __frcp_rn(T.rhoi);
+        T.pri = a.w;
+        MSum s{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const int cnt = A.use_lists ? A.nbr_cnt[i] : -1;
+        if (cnt >= 0) {
+            // four neighbours' loads in flight before their arithmetic
+            int q = 0;
+            for (; q + 4 <= cnt; q += 4) {
+                int jj[4];
+                float4 pp[4], vv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) jj[u] = A.nbr[(size_t)(q + u) * P.N + i];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    pp[u] = A.ms0[jj[u]];
+                    vv[u] = A.ms1[jj[u]];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) msum_add(P, s, T, pp[u], vv[u]);
+            }
+            for (; q < cnt; ++q) {
+                const int j = A.nbr[(size_t)q * P.N + i];
+                msum_add(P, s, T, A.ms0[j], A.ms1[j]);
+            }
+        } else {
+            s = momentum_target_global(P, A, T);
+        }
+        const float3 mi = momentum_epilogue(P, A.out, i, T, s, (mode & M_INTEGRATE) != 0, dt);
+        m = make_float3(fmaxf(m.x, mi.x), fmaxf(m.y, mi.y), fmaxf(m.z, mi.z));
+    }
+}
+
+// The M_RAIN_CELLS x M_TPB rain cells of rain chunk `rc`.
+__device__ __forceinline__ void rain_chunk(const Phys& P, const MArgs& A, int rc, bool aborted, float dt) {
+#pragma unroll
+    for (int r = 0; r < M_RAIN_CELLS; ++r) {
+        const int cid = (rc * M_RAIN_CELLS + r) * M_TPB + threadIdx.x;
+        if (cid < P.ncell && !aborted) rain_cell(P, cid, dt, A.rain_in, A.rain_delta, A.rain_out, A.precip);
+    }
+}
+
 template <int TPT>
 __global__ __launch_bounds__(M_TPB, M_MINB) void k_momentum(const __grid_constant__ Phys P, const __grid_constant__ MArgs A,
                                                     int mode) {
     __shared__ float s_max[3][M_TPB / 32];
-    __shared__ bool s_last;
     DevCtl* ctl = A.ctl;
     const bool aborted = ctl->aborted != 0;
     const float dt = ctl->dt;
-    const bool rain_block = (int)blockIdx.x >= A.part_blocks;
     float3 m = make_float3(0.f, 0.f, 0.f);
-    if (rain_block) {
-#pragma unroll
-        for (int r = 0; r < M_RAIN_CELLS; ++r) {
-            const int cid = ((blockIdx.x - A.part_blocks) * M_RAIN_CELLS + r) * M_TPB + threadIdx.x;
-            if (cid < P.ncell && !aborted) rain_cell(P, cid, dt, A.rain_in, A.rain_delta, A.rain_out, A.precip);
-        }
+    const int chunks = A.part_blocks + A.rain_blocks;
+    if ((int)blockIdx.x >= A.part_blocks) {
+        if ((int)blockIdx.x < chunks) rain_chunk(P, A, blockIdx.x - A.part_blocks, aborted, dt);
     } else {
-        // TPT targets per thread, the lanes of warp w on targets w * 32 * TPT + lane + 32 r:
-        // a warp waits on the longest sum of its lanes' lists rather than on the longest list
-        // of each round; a warp covers 32 TPT consecutive targets, about 32 TPT / ppc cells
-        const int tbase = blockIdx.x * (M_TPB * TPT) + (threadIdx.x >> 5) * (32 * TPT) + (threadIdx.x & 31);
-        for (int r = 0; r < TPT; ++r) {
-            const int i = tbase + 32 * r;
-            if (i < P.N) {
-                if (aborted) {
-                    if (mode & M_INTEGRATE) A.out.vel_out[i] = A.vel[i];
-                } else {
-                    // (x, y, z, p') and (u, v, w, rho): packed by the density pass
-                    // when the lists are current, else from the state buffers
-                    float4 a, b;
-                    if (A.use_lists) {
-                        a = A.ms0[i];
-                        b = A.ms1[i];
-                    } else {
-                        const float4 p = A.pos[i], v = A.vel[i];
-                        const float2 r = A.rp[i];
-                        a = make_float4(p.x, p.y, p.z, r.y);
-                        b = make_float4(v.x, v.y, v.z, r.x);
-                    }
-                    MTarget T;
-                    T.x = a.x; T.y = a.y; T.z = a.z;
-                    T.u = b.x; T.v = b.y; T.w = b.z;
-                    T.rhoi = fmaxf(b.w, 1e-3f);
-                    T.irhoi = __frcp_rn(T.rhoi);
-                    T.pri = a.w;
-                    MSum s{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                    const int cnt = A.use_lists ? A.nbr_cnt[i] : -1;
-                    if (cnt >= 0) {
-                        // four neighbours' loads in flight before their arithmetic
-                        int q = 0;
-                        for (; q + 4 <= cnt; q += 4) {
-                            int jj[4];
-                            float4 pp[4], vv[4];
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) jj[u] = A.nbr[(size_t)(q + u) * P.N + i];
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                pp[u] = A.ms0[jj[u]];
-                                vv[u] = A.ms1[jj[u]];
-                            }
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) msum_add(P, s, T, pp[u], vv[u]);
-                        }
-                        for (; q < cnt; ++q) {
-                            const int j = A.nbr[(size_t)q * P.N + i];
-                            msum_add(P, s, T, A.ms0[j], A.ms1[j]);
-                        }
-                    } else {
-                        s = momentum_target_global(P, A, T);
-                    }
-                    const float3 mi = momentum_epilogue(P, A.out, i, T, s, (mode & M_INTEGRATE) != 0, dt);
-                    m = make_float3(fmaxf(m.x, mi.x), fmaxf(m.y, mi.y), fmaxf(m.z, mi.z));
-                }
-            }
-        }
-        if (mode & M_INTEGRATE) {
+        momentum_chunk<TPT>(P, A, mode, blockIdx.x, aborted, dt, m);
+        if (mode & M_INTEGRATE) {   // the particle blocks' velocity maxima
             float mx = warp_max(m.x), my = warp_max(m.y), mz = warp_max(m.z);
             const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
             if (lane == 0) { s_max[0][warp] = mx; s_max[1][warp] = my; s_max[2][warp] = mz; }
@@ -768,20 +783,14 @@ __global__ __launch_bounds__(M_TPB, M_MINB) void k_momentum(const __grid_constan
             }
         }
     }
-    if (mode & M_CFL) {
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            const unsigned t = atomicAdd(&ctl->done, 1u);
-            s_last = (t == gridDim.x - 1);
-        }
-        __syncthreads();
-        if (s_last && threadIdx.x == 0) {
-            __threadfence();
-            ctl->done = 0u;
-            if (!ctl->aborted) cfl_control(P, ctl);
-        }
-    }
+}
+
+// The CFL control after a momentum pass (asph_h100.cu:1040-1078), in a
+// kernel of its own: one launch costs less than a finished-block atomic from
+// each of the pass's ~11,600 blocks to find the last one (momentum 0.242 ->
+// 0.234 ms at 2M).
+__global__ void k_cfl_final(const __grid_constant__ Phys P, DevCtl* ctl) {
+    if (threadIdx.x == 0 && !ctl->aborted) cfl_control(P, ctl);
 }
 
 // ===========================================================================
@@ -1010,6 +1019,7 @@ void launch_momentum(const Phys& P, const Bufs& B, int mode, int use_lists, cuda
     const int tpt = momentum_tpt(B);
     A.part_blocks = blocks_for(P.N, M_TPB * tpt);
     const int rain_blocks = (mode & M_RAIN) ? blocks_for(P.ncell, M_TPB * M_RAIN_CELLS) : 0;
+    A.rain_blocks = rain_blocks;
     const int grid = A.part_blocks + rain_blocks;
     if (tpt == 1)
         k_momentum<1><<<grid, M_TPB, 0, s>>>(P, A, mode);
@@ -1017,6 +1027,7 @@ void launch_momentum(const Phys& P, const Bufs& B, int mode, int use_lists, cuda
         k_momentum<4><<<grid, M_TPB, 0, s>>>(P, A, mode);
     else
         k_momentum<2><<<grid, M_TPB, 0, s>>>(P, A, mode);
+    if (mode & M_CFL) k_cfl_final<<<1, 32, 0, s>>>(P, A.ctl);
 }
 
 }  // namespace asph

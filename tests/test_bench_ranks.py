@@ -106,7 +106,11 @@ def test_other_workloads_and_options():
     big = bench.workload_params("large16m")
     assert big.n_particles == 256 ** 3 and (big.nx, big.ny, big.nz) == (250, 250, 500)
     assert big.dx / big.dz == pytest.approx(8.0)
-    for name in ("bubble2m", "bubble524k", "reference128", "large16m"):
+    small = bench.workload_params("large2m")   # the large run's cells and density at 2M
+    assert (small.dx, small.dz) == (big.dx, big.dz) and small.n_particles == 128 ** 3
+    assert small.n_particles / (small.nx * small.ny * small.nz) == pytest.approx(
+        big.n_particles / (big.nx * big.ny * big.nz))
+    for name in ("bubble2m", "bubble524k", "reference128", "large16m", "large2m"):
         assert bench.workload_string(name)
         assert bench.metric_for(bench.workload_params(name)).startswith("particle-steps/s (plain step, ")
     assert bench.metric_for(bench.workload_params("bubble2m")) == bench.METRIC   # the headline metric string

@@ -552,13 +552,14 @@ def test_step_kernels_count_the_step_graph():
     """The kernel launches of a step, read from the captured graph: the sort preparation,
     both sorts (the full one a graph branch; a histogram and 3 passes each at 18-bit keys, plus
     the incremental sort's count, scan, split and merge), the gather, the density pass and its
-    deferred kernel, and momentum.  A step in the middle of a run that sorts ahead has the same
-    kernels plus the reset of the sort's histograms that the preparation does otherwise."""
+    deferred kernel, momentum and the CFL control.  A step in the middle of a run that sorts
+    ahead has the same kernels plus the reset of the sort's histograms that the preparation
+    does otherwise."""
     p = small_config(lat=(24, 24, 24), grid=(30, 30, 60), box=(6000.0, 6000.0, 3000.0), sort_every=1)
     sim = Asph(p)
     sim.init()
     passes = (3 * 6 + 7) // 8      # 6 bits per axis at 60 cells
-    plain = 1 + (1 + passes) + (4 + 1 + passes) + 1 + 2 + 1
+    plain = 1 + (1 + passes) + (4 + 1 + passes) + 1 + 2 + 1 + 1
     n0 = sim.step_kernels()        # captured without running
     sim.step(3)
     assert n0 == sim.step_kernels() == plain + 1
