@@ -371,20 +371,15 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
         }
     }
     if (staged) {
-        // slots strided over the block, four loads in flight per thread
-        for (int kb = threadIdx.x; kb < total; kb += 4 * T) {
-            float4 q[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int k = kb + u * T;
-                if (k < total) q[u] = A.pos[s_gidx[k]];
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int k = kb + u * T;
-                if (k < total) sp[k] = q[u];
-            }
+        // slots strided over the block, copied global -> shared asynchronously:
+        // every slot of the thread in flight at once, no registers held (density
+        // 0.538 -> 0.527 ms at 2M against four register loads in flight)
+        for (int k = threadIdx.x; k < total; k += T) {
+            const unsigned d = (unsigned)__cvta_generic_to_shared(sp + k);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(A.pos + s_gidx[k]) : "memory");
         }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     }
     __syncthreads();
 
