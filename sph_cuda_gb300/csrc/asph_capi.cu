@@ -972,7 +972,12 @@ static int capture_step_graph(asph_ctx* c, int kind) {
     const Bufs saved = c->B;
     cudaGraph_t g = nullptr;
     CKR(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_step(c, kind);
+    if (kind == STEP_MID2) {   // two middle steps in one graph
+        enqueue_step(c, STEP_MID);
+        enqueue_step(c, STEP_MID);
+    } else {
+        enqueue_step(c, kind);
+    }
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     c->B = saved;
     if (e != cudaSuccess) return fail(ASPH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
@@ -1022,16 +1027,20 @@ extern "C" int asph_step_async(asph_ctx* c, int nsteps) {
     if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
     if (!c->initialised) return fail(ASPH_ERR_STATE, "step before init/set_state");
     ensure_spans(c);
-    for (int k = 0; k < nsteps; ++k) {
-        const int kind = step_kind(c, k, nsteps);
+    for (int k = 0; k < nsteps;) {
+        int kind = step_kind(c, k, nsteps), adv = 1;
+        // two middle steps per graph launch: one inter-graph gap fewer per pair
+        // (524k: 0.270 -> 0.267 ms per step)
+        if (kind == STEP_MID && k + 2 <= nsteps - 1) { kind = STEP_MID2; adv = 2; }
         const int slot = kind * 16 + graph_slot(c->B);
         if (!c->gexec[slot]) {
             const int st = capture_step_graph(c, kind);
             if (st) return st;
         }
         CKR(cudaGraphLaunch(c->gexec[slot], c->stream));
-        c->B.pc ^= 1; c->B.qc ^= 1; c->B.rc ^= 1;   // vel flips twice per step
+        for (int a = 0; a < adv; ++a) { c->B.pc ^= 1; c->B.qc ^= 1; c->B.rc ^= 1; }   // vel flips twice per step
         c->lists_valid = true;
+        k += adv;
     }
     return ASPH_OK;
 }

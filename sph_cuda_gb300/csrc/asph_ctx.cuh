@@ -18,8 +18,8 @@ struct asph_ctx {
     bool lists_valid = false;   // neighbour lists match the current positions
     bool spans_valid = false;   // brick spans match the sorted keys and the brick shape in use
     // step graphs keyed by kind (StepKind) x the ping-pong state at the start of the step
-    cudaGraphExec_t gexec[4 * 16] = {};
-    int graph_kernels[4] = {};  // kernel nodes of a captured step graph of each kind
+    cudaGraphExec_t gexec[5 * 16] = {};
+    int graph_kernels[5] = {};  // kernel nodes of a captured step graph of each kind
     bool sort_ahead = true;     // ASPH_OPT_SORT_AHEAD
     unsigned graph_epoch = 0;   // bumped whenever an option change drops the captured graphs
     // staging for host <-> device SoA copies (16 floats per particle)
@@ -78,8 +78,9 @@ int sync_status(asph_ctx* c);
 // its start and also sorts the next step's keys beside its pair passes, the
 // middle steps (STEP_MID) apply the sort run ahead and run the next one, and
 // the last (STEP_LAST) applies the sort run ahead and runs none, so that
-// between calls the context holds the last applied sort.
-enum StepKind : int { STEP_PLAIN = 0, STEP_FIRST = 1, STEP_MID = 2, STEP_LAST = 3 };
+// between calls the context holds the last applied sort.  STEP_MID2 is two
+// middle steps captured in one graph.
+enum StepKind : int { STEP_PLAIN = 0, STEP_FIRST = 1, STEP_MID = 2, STEP_LAST = 3, STEP_MID2 = 4 };
 // Enqueue one full step (sort, gather/kick/drift/flux, density, momentum)
 // on the context's stream and advance the ping-pong indices.
 void enqueue_step(asph_ctx* c, int kind = STEP_PLAIN);
