@@ -261,7 +261,6 @@ __device__ __forceinline__ void msum_add(const Phys& P, MSum& s, const MTarget& 
     const float t2 = 2.0f - q;
     // dW/dq / q: inner branch sigma (2.25 q - 3), outer -0.75 sigma (2 - q)^2 / q
     const float k = q < 1.0f ? SIGMA_W * __fmaf_rn(2.25f, q, -3.0f) : (-0.75f * SIGMA_W) * (t2 * t2) * rs;
-    const float gx = (k * P.inv_dx) * dxt, gy = (k * P.inv_dy) * dyt, gz = (k * P.inv_dz) * dzt;
     const float rhoj = fmaxf(vj.w, 1e-3f);
     const float irj = __fdividef(1.0f, rhoj);
     const float dp = (pj.w - T.pri) * (T.irhoi * irj);
@@ -276,8 +275,11 @@ __device__ __forceinline__ void msum_add(const Phys& P, MSum& s, const MTarget& 
         visc = (mu * __fmaf_rn(P.beta, mu, -P.alpha * P.cs)) * __fdividef(irj, rbar * rbar);
     }
     const float br = dp + visc;
-    s.ax = __fmaf_rn(-br, gx, s.ax); s.ay = __fmaf_rn(-br, gy, s.ay); s.az = __fmaf_rn(-br, gz, s.az);
-    s.vx = __fmaf_rn(-visc, gx, s.vx); s.vy = __fmaf_rn(-visc, gy, s.vy); s.vz = __fmaf_rn(-visc, gz, s.vz);
+    // grad_i W = k (dxt inv_dx, dyt inv_dy, dzt inv_dz): the sums carry k (dxt, dyt, dzt)
+    // and the epilogue applies inv_d once per target (4 products fewer per pair)
+    const float ck = -br * k, cv = -visc * k;
+    s.ax = __fmaf_rn(ck, dxt, s.ax); s.ay = __fmaf_rn(ck, dyt, s.ay); s.az = __fmaf_rn(ck, dzt, s.az);
+    s.vx = __fmaf_rn(cv, dxt, s.vx); s.vy = __fmaf_rn(cv, dyt, s.vy); s.vz = __fmaf_rn(cv, dzt, s.vz);
 }
 
 // Momentum epilogue: mass scaling, buoyancy with condensate loading,
@@ -293,8 +295,10 @@ struct MOut {
 };
 __device__ __forceinline__ float3 momentum_epilogue(const Phys& P, const MOut& O, int i, const MTarget& T, MSum s,
                                                     bool integrate, float dt) {
-    s.ax *= P.mm; s.ay *= P.mm; s.az *= P.mm;
-    s.vx *= P.mm; s.vy *= P.mm; s.vz *= P.mm;
+    // mass scaling and the gradient's per-axis factor (msum_add leaves it out)
+    const float mx = P.mm * P.inv_dx, my = P.mm * P.inv_dy, mz = P.mm * P.inv_dz;
+    s.ax *= mx; s.ay *= my; s.az *= mz;
+    s.vx *= mx; s.vy *= my; s.vz *= mz;
     float4 ti = O.thq[i];
     // theta_v - theta_v,ref without cancellation: (th - thvr) + 0.608 th qv
     const FF vr = snd_eval(P.snd_thvr, P.snd_n, T.z);
