@@ -45,3 +45,36 @@ def test_pinned_and_pageable_state_exchange_agree():
         assert np.array_equal(sb[k], sc[k]), k
     for sim in (a, b, c):
         sim.close()
+
+
+def _pinned_offset(a, off):
+    """A pinned copy of `a` that starts `off` floats into its allocation (off = 1:
+    not 16-byte aligned)."""
+    torch = pytest.importorskip("torch")
+    t = torch.empty(a.shape[0] + 4, dtype=torch.float32, pin_memory=True).numpy()[off:off + a.shape[0]]
+    t[...] = a
+    return t
+
+
+@pytest.mark.gpu
+def test_pinned_exchange_ragged_count_and_unaligned_arrays():
+    """A particle count that is not a multiple of 4, with 16-byte aligned
+    pinned arrays and with arrays that start one float into their pinned
+    allocation: set and get return the state they were given."""
+    p = small_config(lat=(15, 15, 15), grid=(20, 20, 40))
+    assert p.n_particles % 4 == 3
+    s = {k: v for k, v in random_state(p, seed=5, layout="uniform").items()}
+    ref = Asph(p)
+    ref.set_state(s)
+    want = ref.get_state()
+    for off in (0, 1):
+        sim = Asph(p)
+        sim.set_state({k: _pinned_offset(np.asarray(v, np.float32), off) for k, v in want.items()})
+        back = sim.get_state()
+        out = {k: _pinned_offset(np.zeros(p.n_particles, np.float32), off) for k in STATE_FIELDS}
+        got = sim.get_state(STATE_FIELDS, out=out)
+        for k in STATE_FIELDS:
+            assert np.array_equal(back[k], want[k]), (off, k)
+            assert np.array_equal(got[k], want[k]), (off, k)
+        sim.close()
+    ref.close()
