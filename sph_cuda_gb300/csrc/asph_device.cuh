@@ -126,18 +126,19 @@ __device__ __forceinline__ void rain_cell(const Phys& P, int cid, float dt, cons
     if (iz == 0) atomicAdd(&precip[iy * P.nx + ix], outMass / (P.dx * P.dy));
 }
 
-// Density pair sums of one target: S1 = sum W, S2 = sum W/rho_j,
+// Density pair sums of one target, in units of SIGMA_W / 4: S1 = sum W, S2 = sum W/rho_j,
 // T = sum W (rho_j - rho_ref(z_i)) / rho_j  (= S1 - rho_ref S2 without the
 // cancellation).  Self pair included (asph_h100.cu:314-325).
 struct DSum {
     float S1, S2, T;
 };
 __device__ __forceinline__ void dsum_add(DSum& s, float r2, float rho_j, const FF& rr) {
-    // accepted pairs only (r2 < 4): the spline of w3 in Horner form with FMAs
+    // accepted pairs only (r2 < 4): the spline of w3 in Horner form with FMAs,
+    // scaled by 4 / SIGMA_W (4 - 6 q^2 + 3 q^3 inside, (2 - q)^3 outside): the
+    // epilogue uses the sums only as the ratios S1 / S2 and T / S2
     const float q = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
     const float t = 2.0f - q;
-    const float W = q < 1.0f ? SIGMA_W * __fmaf_rn(q * q, __fmaf_rn(0.75f, q, -1.5f), 1.0f)
-                             : (0.25f * SIGMA_W) * (t * t * t);
+    const float W = q < 1.0f ? __fmaf_rn(q * q, __fmaf_rn(3.0f, q, -6.0f), 4.0f) : t * t * t;
     const float rj = fmaxf(rho_j, 1e-3f);
     const float iw = __fdividef(W, rj);
     s.S1 += W;
