@@ -409,14 +409,19 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
             if (active && !fast) A.defer[at + __popc(dm & ((1u << lane) - 1u))] = i;
         }
         NbrOut L{A.nbr, 0, P.N, i};
+        // the lanes' queues are the columns of the DLIST x T array (entry e of
+        // this lane at qlane[e T]); n counts the queued entries in units of T,
+        // so a push is one store and one add (density 0.5255 -> 0.5194 ms at 2M
+        // against indexing by the entry count)
+        unsigned short* const qlane = s_list + threadIdx.x;
+        const int qlim = (C.dlist - 4) * T;
         int n = 0;
-        // all lanes drain their queues together, in lockstep
 #define ASPH_DRAIN()                                                                  \
     do {                                                                              \
         const int nmax_ = __reduce_max_sync(0xffffffffu, n);                          \
-        for (int q = 0; q < nmax_; ++q) {                                             \
+        for (int q = 0; q < nmax_; q += T) {                                          \
             if (q < n) {                                                              \
-                const int kq = s_list[q * T + threadIdx.x];                           \
+                const int kq = qlane[q];                                              \
                 const float4 pj = sp[kq];                                             \
                 const float r2 = r2_pair(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z);      \
                 dsum_add(s, r2, pj.w, rr);                                            \
@@ -458,11 +463,13 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
                 }
                 const bool valid = k < kend;
                 const float4 pj = sp[valid ? k : 0];
-                if (valid && r2_pair(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z) < 4.0f)
-                    s_list[(n++) * T + threadIdx.x] = (unsigned short)k;
+                if (valid && r2_pair(P, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z) < 4.0f) {
+                    qlane[n] = (unsigned short)k;
+                    n += T;
+                }
                 k += valid ? 1 : 0;
             }
-            if (__any_sync(0xffffffffu, n > C.dlist - 4)) ASPH_DRAIN();
+            if (__any_sync(0xffffffffu, n > qlim)) ASPH_DRAIN();
             if (__all_sync(0xffffffffu, la >= la_end)) break;
         }
         ASPH_DRAIN();
