@@ -920,6 +920,7 @@ extern "C" int asph_set_viscosity(asph_ctx* c, float alpha, float beta) {
     if (!c) return fail(ASPH_ERR_ARG, "ctx is NULL");
     c->P.alpha = alpha;
     c->P.beta = beta;
+    set_viscosity_terms(c->P);
     c->prm.alpha_av = alpha;
     c->prm.beta_av = beta;
     for (auto& g : c->gexec)

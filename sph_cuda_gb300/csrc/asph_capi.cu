@@ -204,6 +204,7 @@ static void derive(const AsphParams& p, Phys& P) {
     P.alpha = p.alpha_av; P.beta = p.beta_av;
     P.h_av = p.h_av > 0.f ? p.h_av : 2.0f * p.dz;
     P.eta2 = (0.01f * P.h_av) * (0.01f * P.h_av);
+    asph::set_viscosity_terms(P);
     P.sponge_sigma = p.sponge_sigma; P.sponge_frac = p.sponge_frac; P.dthdt_cap = p.dthdt_cap;
     P.surface_flux = p.surface_flux;
     P.c_h = p.c_h; P.c_e = p.c_e; P.beta_moist = p.beta_moist; P.v_bg = p.v_bg; P.dts_skin = p.dts_skin;

@@ -260,8 +260,8 @@ __device__ __forceinline__ void msum_add(const Phys& P, MSum& s, const MTarget& 
     const float rs = rsqrtf(r2t);
     const float q = r2t * rs;
     const float t2 = 2.0f - q;
-    // dW/dq / q: inner branch sigma (2.25 q - 3), outer -0.75 sigma (2 - q)^2 / q
-    const float k = q < 1.0f ? SIGMA_W * __fmaf_rn(2.25f, q, -3.0f) : (-0.75f * SIGMA_W) * (t2 * t2) * rs;
+    // dW/dq / q in units of -0.75 SIGMA_W: inner 4 - 3 q, outer (2 - q)^2 / q
+    const float k = q < 1.0f ? __fmaf_rn(-3.0f, q, 4.0f) : (t2 * t2) * rs;
     const float rhoj = fmaxf(vj.w, 1e-3f);
     const float irj = __fdividef(1.0f, rhoj);
     const float dp = (pj.w - T.pri) * (T.irhoi * irj);
@@ -270,10 +270,11 @@ __device__ __forceinline__ void msum_add(const Phys& P, MSum& s, const MTarget& 
     float visc = 0.f;
     if (vdotr < 0.f) {
         const float rp2 = __fmaf_rn(rx, rx, __fmaf_rn(ry, ry, rz * rz));
-        const float rbar = 0.5f * (T.rhoi + rhoj);
-        // (-alpha cs mu + beta mu^2) / (rbar^2 rho_j), mu = h vdotr / (r^2 + eta^2)
-        const float mu = __fdividef(P.h_av * vdotr, rp2 + P.eta2);
-        visc = (mu * __fmaf_rn(P.beta, mu, -P.alpha * P.cs)) * __fdividef(irj, rbar * rbar);
+        // (-alpha cs mu + beta mu^2) / (rbar^2 rho_j) with mu = h m, m = vdotr / (r^2 + eta^2),
+        // rbar = s / 2: m (4 beta h^2 m - 4 alpha cs h) / (s^2 rho_j)
+        const float m = __fdividef(vdotr, rp2 + P.eta2);
+        const float is = __fdividef(1.0f, T.rhoi + rhoj);
+        visc = (m * __fmaf_rn(P.av_quad, m, P.av_lin)) * (irj * (is * is));
     }
     const float br = dp + visc;
     // grad_i W = k (dxt inv_dx, dyt inv_dy, dzt inv_dz): the sums carry k (dxt, dyt, dzt)
@@ -297,7 +298,8 @@ struct MOut {
 __device__ __forceinline__ float3 momentum_epilogue(const Phys& P, const MOut& O, int i, const MTarget& T, MSum s,
                                                     bool integrate, float dt) {
     // mass scaling and the gradient's per-axis factor (msum_add leaves it out)
-    const float mx = P.mm * P.inv_dx, my = P.mm * P.inv_dy, mz = P.mm * P.inv_dz;
+    const float mk = P.mm * (-0.75f * SIGMA_W);   // msum_add's k is in units of -0.75 SIGMA_W
+    const float mx = mk * P.inv_dx, my = mk * P.inv_dy, mz = mk * P.inv_dz;
     s.ax *= mx; s.ay *= my; s.az *= mz;
     s.vx *= mx; s.vy *= my; s.vz *= mz;
     float4 ti = O.thq[i];

@@ -246,10 +246,15 @@ __device__ int region_offsets(const Phys& P, const int2* __restrict__ range, int
 
 // Neighbour-list writer of one target (slot-major, coalesced over targets).
 struct NbrOut {
-    int* nbr;
-    int n, N, i;
+    int* p;      // the next slot of target i's list
+    size_t N;    // slot stride
+    int n;
+    __device__ __forceinline__ NbrOut(int* nbr, int n0, int N_, int i) : p(nbr + i), N((size_t)N_), n(n0) {}
     __device__ __forceinline__ void push(int j) {
-        if (n < NBR_CAP) nbr[(size_t)n * N + i] = j;
+        if (n < NBR_CAP) {
+            *p = j;
+            p += N;
+        }
         ++n;
     }
 };
@@ -722,11 +727,14 @@ __device__ __forceinline__ void momentum_chunk(const Phys& P, const MArgs& A, in
         if (cnt >= 0) {
             // four neighbours' loads in flight before their arithmetic
             int q = 0;
+            const int* lp = A.nbr + i;   // slot q of the list at lp[q N]
+            const size_t N = (size_t)P.N;
             for (; q + 4 <= cnt; q += 4) {
                 int jj[4];
                 float4 pp[4], vv[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) jj[u] = A.nbr[(size_t)(q + u) * P.N + i];
+                for (int u = 0; u < 4; ++u) jj[u] = lp[u * N];
+                lp += 4 * N;
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     pp[u] = A.ms0[jj[u]];
@@ -736,7 +744,8 @@ __device__ __forceinline__ void momentum_chunk(const Phys& P, const MArgs& A, in
                 for (int u = 0; u < 4; ++u) msum_add(P, s, T, pp[u], vv[u]);
             }
             for (; q < cnt; ++q) {
-                const int j = A.nbr[(size_t)q * P.N + i];
+                const int j = *lp;
+                lp += N;
                 msum_add(P, s, T, A.ms0[j], A.ms1[j]);
             }
         } else {

@@ -41,6 +41,7 @@ struct Phys {
     float qv0, rh, rh_bl, z_bl;
     // dissipation
     float alpha, beta, h_av, eta2;  // eta2 = (0.01 h_av)^2 (asph_h100.cu:482)
+    float av_lin, av_quad;          // -4 alpha cs h_av and 4 beta h_av^2 (set_viscosity_terms)
     float sponge_sigma, sponge_frac, dthdt_cap;
     // surface
     int   surface_flux;
@@ -62,6 +63,12 @@ struct Phys {
     const float4* snd_thvr;   // theta_ref * (1 + 0.608 qv_ref)
     int   snd_n;              // nodes
 };
+
+// Viscosity constants of the momentum pair term, from alpha, beta, cs, h_av.
+inline void set_viscosity_terms(Phys& P) {
+    P.av_lin = -4.0f * P.alpha * P.cs * P.h_av;
+    P.av_quad = 4.0f * P.beta * P.h_av * P.h_av;
+}
 
 // ---- SPH kernel (asph_h100.cu:125-134) -----------------------------------
 AHD float w3(float q) {
