@@ -127,8 +127,8 @@ __device__ __forceinline__ void rain_cell(const Phys& P, int cid, float dt, cons
 }
 
 // Density pair sums of one target, in units of SIGMA_W / 4: S1 = sum W, S2 = sum W/rho_j,
-// T = sum W (rho_j - rho_ref(z_i)) / rho_j  (= S1 - rho_ref S2 without the
-// cancellation).  Self pair included (asph_h100.cu:314-325).
+// T = sum W (rho_j - hi) / rho_j with rho_ref(z_i) = hi + lo (T - lo S2 = S1 - rho_ref S2
+// without the cancellation).  Self pair included (asph_h100.cu:314-325).
 struct DSum {
     float S1, S2, T;
 };
@@ -143,7 +143,7 @@ __device__ __forceinline__ void dsum_add(DSum& s, float r2, float rho_j, const F
     const float iw = __fdividef(W, rj);
     s.S1 += W;
     s.S2 += iw;
-    s.T = fmaf(iw, (rj - rr.hi) - rr.lo, s.T);
+    s.T = fmaf(iw, rj - rr.hi, s.T);   // rho_ref's low part enters once, in the epilogue
 }
 
 // Density result + EOS + saturation adjustment + autoconversion (+ Kessler
@@ -166,7 +166,7 @@ __device__ __forceinline__ void density_eos_epilogue(const Phys& P, const DOut& 
     if (s.S2 > 1e-20f) {
         const float raw = s.S1 / s.S2;
         rho = fminf(fmaxf(raw, 0.5f * rref), 2.0f * rref);
-        dd = (rho == raw) ? s.T / s.S2 : rho - rref;
+        dd = (rho == raw) ? s.T / s.S2 - rr.lo : rho - rref;
     } else {
         rho = fminf(fmaxf(rref, 0.5f * rref), 2.0f * rref);
         dd = 0.f;
