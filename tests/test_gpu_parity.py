@@ -298,8 +298,12 @@ def test_init_matches_reference_kernels():
 # ---------------------------------------------------------------------------
 # the fused, graph-captured step
 # ---------------------------------------------------------------------------
-def test_graph_step_equals_granular_blocks():
-    p, s = _case("ref_jitter")
+@pytest.mark.parametrize("name", ["ref_jitter", "cfg_jitter", "cfg_wide_cluster", "ref_fast"])
+def test_graph_step_equals_granular_blocks(name):
+    """The graph step equals the granular entry points bit for bit: small
+    drifts, clustered regions (split), drifts of more than a cell (deferred
+    targets)."""
+    p, s = _case(name)
     a = _ctx(p, s)
     b = _ctx(p, s)
     a.step(1)
