@@ -743,10 +743,19 @@ __device__ __forceinline__ void momentum_chunk(const Phys& P, const MArgs& A, in
 #pragma unroll
                 for (int u = 0; u < 4; ++u) msum_add(P, s, T, pp[u], vv[u]);
             }
-            for (; q < cnt; ++q) {
-                const int j = *lp;
-                lp += N;
-                msum_add(P, s, T, A.ms0[j], A.ms1[j]);
+            if (q < cnt) {   // the last 1-3 neighbours as one batch, their loads in flight together
+                int jj[3];
+                float4 pp[3], vv[3];
+#pragma unroll
+                for (int u = 0; u < 3; ++u) jj[u] = q + u < cnt ? lp[u * N] : i;
+#pragma unroll
+                for (int u = 0; u < 3; ++u) {
+                    pp[u] = A.ms0[jj[u]];
+                    vv[u] = A.ms1[jj[u]];
+                }
+#pragma unroll
+                for (int u = 0; u < 3; ++u)
+                    if (q + u < cnt) msum_add(P, s, T, pp[u], vv[u]);
             }
         } else {
             s = momentum_target_global(P, A, T);
