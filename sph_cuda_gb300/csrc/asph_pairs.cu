@@ -421,6 +421,7 @@ __device__ __forceinline__ void density_region(const Phys& P, const DArgs& A, co
         unsigned short* const qlane = s_list + threadIdx.x;
         const int qlim = (C.dlist - 4) * T;
         int n = 0;
+        // all lanes drain their queues together, in lockstep
 #define ASPH_DRAIN()                                                                  \
     do {                                                                              \
         const int nmax_ = __reduce_max_sync(0xffffffffu, n);                          \
